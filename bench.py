@@ -1,0 +1,335 @@
+"""Benchmark of the explicit phase-field step on GB300.
+
+Workload: spheres256_lognormal5_vf30 -- a 256^3 periodic grid, seeded
+non-overlapping spheres with lognormal radii (median 5 cells, sigma 0.3) at
+solid fraction 0.3, tanh interfaces of width 4, c at the common-tangent
+compositions +- 1e-3; dt = 0.8 of the explicit limit.  FP32 fused stencil.
+
+One bench step = 100 explicit time steps followed by the FP64 reductions
+(mass, phase fraction, free energy, last-step increment sums) read back to
+the host.  value = cells * time steps / second over the K timed bench steps
+(GLUPS), device-timed with CUDA events on the stream the kernels run on.
+The state (2 x 3 x 67 MB) is larger than L2, so no flush is needed.
+
+e2e: the same metric through the C-ABI with host buffers: each step uploads
+the state from pinned host memory (ppf_upload), advances 100 steps,
+reduces and downloads the state (ppf_download).
+
+--impl reference: the reference program itself (phasefield.c, serial build
+with OpenMP on its three passes, oracle/build_ref.py) on the host cores,
+same workload; each step is one run of 10 time steps timed by the
+program's own loop timer.
+
+Multi-GPU: replicas only (one independent domain per rank), max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "sim-time per wall-s @256^3: surrogate vs plain stencil at <=1% R-bar err; GLUPS"
+WORKLOAD = "spheres256_lognormal5_vf30"
+DT_LIMIT = 1.0 / (6.0 * 1e-14)
+DT = 0.8 * DT_LIMIT
+INNER = 100
+ALG_BYTES_F32 = 24          # read etaS, etaL, c + write 3, float
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in open(self.path):
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def read_profile_traffic():
+    """dram bytes per launch of the f32 step from the committed ncu summary."""
+    p = os.path.join(REPO, "profiles", "step_f32_spheres256.md")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.startswith("dram_bytes_per_launch_256:"):
+            try:
+                return float(ln.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline_sample(state, cells):
+    """The reference program (or, where it cannot be built, the oracle
+    restatement) on a bounded sample of the same workload."""
+    import oracle.build_ref as br
+    import __graft_entry__ as ge
+    ncores = os.cpu_count() or 1
+    try:
+        exe = br.build(**ge.REF_BENCH)
+        from phasefield_coarsening_gb300 import write_fields
+        with tempfile.TemporaryDirectory() as td:
+            inp = os.path.join(td, "in.h5")
+            write_fields(inp, *state)
+            r = br.run(exe, inp, threads=ncores, timeout=1200)
+        if r["rc"] == 0 and r["loop_s"]:
+            steps = ge.REF_BENCH["n_iter"]
+            return {"value": cells * steps / r["loop_s"] / 1e9, "unit": "GLUPS", "cores": ncores,
+                    "kind": "reference",
+                    "sample": f"{steps} time steps of the 256^3 workload, reference phasefield.c serial build "
+                              f"+ OpenMP on sweep_fields, gcc -O2, {ncores} threads"}
+    except Exception as e:  # fall through to the port
+        print(f"reference build unavailable ({e}); timing the oracle restatement", file=sys.stderr)
+    import oracle
+    steps = 5
+    t0 = time.perf_counter()
+    oracle.run(*state, steps, bc=0, params=oracle.reference_params(dt=DT))
+    t = time.perf_counter() - t0
+    return {"value": cells * steps / t / 1e9, "unit": "GLUPS", "cores": ncores, "kind": "port",
+            "sample": f"{steps} time steps of the 256^3 workload, oracle restatement (C, OpenMP), {ncores} threads"}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import phasefield_coarsening_gb300 as ppf
+    from phasefield_coarsening_gb300 import ic
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    eS, eL, c, info = ic.workload(WORKLOAD, seed=args.seed + rank)
+    shape = eS.shape
+    cells = int(np.prod(shape))
+    sim = ppf.Simulation(shape, ppf.params_default(dt=DT), bc="periodic", precision="f32")
+    stream = torch.cuda.current_stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.upload(eS, eL, c)
+
+    def bench_step():
+        sim.step(INNER)
+        return sim.reduce()
+
+    for _ in range(args.warmup):
+        bench_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    stats = None
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        sim.step(INNER)
+        ev[k][1].record(stream)
+        stats = sim.reduce()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = t0.elapsed_time(t1)
+    step_ms = sum(a.elapsed_time(b) for a, b in ev) / (args.steps * INNER)   # per f32 step launch
+    if world > 1:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    value = world * cells * INNER * args.steps / (total_ms * 1e-3) / 1e9
+
+    # e2e through the C-ABI with pinned host buffers
+    host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (eS, eL, c)]
+    outh = [torch.empty(shape, dtype=torch.float64).pin_memory() for _ in range(3)]
+    ptr_in = [h.data_ptr() for h in host]
+    ptr_out = [h.data_ptr() for h in outh]
+
+    def e2e_step():
+        sim.upload_from(*ptr_in)
+        sim.step(INNER)
+        st = sim.reduce()
+        sim.download_into(*ptr_out)
+        return st
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - w0
+    if world > 1:
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e_value = world * cells * INNER * args.steps / e2e_s / 1e9
+
+    if rank == 0:
+        hbm, src = peaks()
+        achieved = ALG_BYTES_F32 * cells / (step_ms * 1e-3) / 1e9
+        traffic = read_profile_traffic()
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": f"synthetic: seeded spheres ({info['particles']} particles, sphere fraction "
+                    f"{info['sphere_fraction']:.3f}), generated on the host",
+            "config": {"workload": WORKLOAD, "grid": list(shape), "bc": "periodic", "dt": DT,
+                       "time_steps_per_bench_step": INNER, "precision": "f32 storage and arithmetic, FP64 reductions",
+                       "l2": "state 403 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+            "sim_time_per_wall_s": round(value * 1e9 / cells * DT, 1),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(achieved / hbm, 4), "traffic": traffic,
+                         "kernel": "step_kernel<float,64,8,256>", "algorithmic_bytes_per_launch": ALG_BYTES_F32 * cells,
+                         "avg_launch_us": round(step_ms * 1e3, 2), "peak_source": src},
+            "e2e": {"value": round(e2e_value, 3), "unit": "GLUPS", "h2d_bytes_per_step": 3 * cells * 8,
+                    "d2h_bytes_per_step": 3 * cells * 8 + 8 * 8},
+            "gpu_launches": args.steps * (INNER + 1 + 2),
+            "clocks": clk,
+            "final_stats": {k: stats[k] for k in ("mass", "solid", "free_energy", "nonfinite")},
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline_sample((eS, eL, c), cells)
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+
+    import oracle.build_ref as br
+    import __graft_entry__ as ge
+    from phasefield_coarsening_gb300 import ic, write_fields
+    ncores = os.cpu_count() or 1
+    try:
+        exe = br.build(**ge.REF_BENCH)
+    except Exception as e:
+        print(json.dumps({"impl": "reference", "unavailable": f"reference build failed: {str(e)[:200]}"}))
+        return
+    eS, eL, c, info = ic.workload(WORKLOAD, seed=args.seed)
+    cells = int(np.prod(eS.shape))
+    steps_per_run = ge.REF_BENCH["n_iter"]
+    with tempfile.TemporaryDirectory() as td:
+        inp = os.path.join(td, "in.h5")
+        write_fields(inp, eS, eL, c)
+        for _ in range(args.warmup):
+            br.run(exe, inp, threads=ncores, timeout=1800)
+        loop = []
+        for _ in range(args.steps):
+            r = br.run(exe, inp, threads=ncores, timeout=1800)
+            if r["rc"] != 0 or not r["loop_s"]:
+                print(json.dumps({"impl": "reference", "unavailable": "reference run failed: " + r["stderr"][-200:]}))
+                return
+            loop.append(r["loop_s"])
+    total = sum(loop)
+    value = cells * steps_per_run * args.steps / total / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "GLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": f"synthetic: seeded spheres ({info['particles']} particles)",
+        "config": {"workload": WORKLOAD, "grid": list(eS.shape), "bc": "periodic", "dt": DT,
+                   "time_steps_per_bench_step": steps_per_run, "parallelism": f"OpenMP x{ncores} (host)"},
+        "sim_time_per_wall_s": round(value * 1e9 / cells * DT, 1),
+        "cpu_baseline": {"value": round(value, 4), "unit": "GLUPS", "cores": ncores, "kind": "reference",
+                         "sample": f"{steps_per_run} time steps per run of the reference phasefield.c "
+                                   f"(serial build + OpenMP on sweep_fields, gcc -O2), {ncores} threads"},
+        "e2e": {"value": round(value, 4), "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("note: warm-up below 3 steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

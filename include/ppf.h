@@ -1,0 +1,159 @@
+/*
+ * ppf.h -- C ABI of the GB300 explicit phase-field step.
+ *
+ * The reference program (jijn/phasefield_coarsening, one C file) has no
+ * library interface: its hot path is the pair of functions
+ *
+ *   sweep_fields   phasefield.c:301-403   full step of etaS, etaL and c
+ *   sweep_fields_c phasefield.c:406-476   c-only step (eta frozen)
+ *
+ * called from the time loop in main (phasefield.c:178-258) after the ghost
+ * layers have been filled by apply_periodic_boundary_condition
+ * (:1112-1148), apply_nonflux_boundary_condition (:1151-1189) or the MPI
+ * halo exchange (:683-708, :762-826).  The state lives in ten global
+ * arrays double[NI+2][NJ+2][NK+2] (:67-70) indexed [z][y][x].
+ *
+ * This header is the drop-in boundary for that path: an opaque context owns
+ * the device copy of the state (3 fields, two ping-pong buffers, one ghost
+ * layer per face); the caller owns host arrays that hold only the interior,
+ * nz*ny*nx values in C order [z][y][x] -- the same order as the /etaS,
+ * /etaL and /c HDF5 datasets the reference reads (:996-1049).
+ *
+ * Conventions:
+ *   - every function returns 0 on success or a negative PPF_E* code;
+ *     ppf_last_error() returns a message for the calling thread's last
+ *     failure;
+ *   - calls on one context are synchronous with respect to the host unless
+ *     the name says _async; one context must not be used from two threads
+ *     at once; contexts are independent of each other;
+ *   - nothing here falls back to the CPU: without a usable CUDA device
+ *     ppf_create fails with PPF_ECUDA.
+ */
+#ifndef PPF_H
+#define PPF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* return codes */
+#define PPF_OK        0
+#define PPF_EINVAL   (-1)   /* bad argument */
+#define PPF_ECUDA    (-2)   /* CUDA runtime/driver error, or no device */
+#define PPF_ENOMEM   (-3)   /* device or host allocation failed */
+#define PPF_ESTATE   (-4)   /* call not valid in the context's state */
+#define PPF_EIO      (-5)   /* file I/O (HDF5 subset) failed */
+#define PPF_ETIMEOUT (-6)   /* a bounded device wait ran out */
+
+/* boundary conditions: the values of USE_BC_TYPE, phasefield.c:15-16 */
+#define PPF_BC_PERIODIC 0   /* ghost = opposite face, :1112-1148 */
+#define PPF_BC_NOFLUX   1   /* ghost = adjacent interior cell, :1151-1189 */
+
+/* storage + arithmetic precision of the step */
+#define PPF_F64 0           /* the reference's double, phasefield.c:67-70 */
+#define PPF_F32 1           /* float storage and arithmetic */
+
+/* Material and numerical constants, phasefield.c:76-97.  Derived values
+ * (ML, MS, h2, m, kappa, L) are computed from these exactly as the
+ * reference does; see ppf_params_derive. */
+typedef struct ppf_params {
+    double AS, AL;      /* parabola curvatures, :76-77 */
+    double CS, CL;      /* parabola offsets, :78-79 */
+    double cS0, cL0;    /* parabola minima, :80-81 */
+    double cSeq, cLeq;  /* compositions used by the mobility L, :82-83 */
+    double DL, DS;      /* diffusivities, :84 */
+    double sigma;       /* interface energy, :87 */
+    double gamma;       /* Moelans gamma, :88 */
+    double dx;          /* grid spacing, :90 */
+    double dt;          /* time step, :92; <= 0 selects 0.125*dx*dx/DL */
+    double l;           /* interface width, :94; <= 0 selects 7*dx */
+} ppf_params;
+
+typedef struct ppf_derived {
+    double ML, MS;      /* DL/AL, DS/AS, :85 */
+    double h2;          /* 1/dx^2, :91 */
+    double dt;          /* effective time step */
+    double l;           /* effective interface width */
+    double m;           /* 6 sigma / l, :95 */
+    double kappa;       /* 3/4 sigma l, :96 */
+    double L;           /* 4/3 m/kappa (MS+ML)/2 / (cSeq-cLeq)^2, :97 */
+    double dt_limit;    /* explicit limit of the solute equation, dx^2/(6 max(DL,DS)) */
+} ppf_derived;
+
+/* Reductions.  The first three are the reference's convergence sums over
+ * the interior (phasefield.c:228-238), taken over the increments of the
+ * most recent step; the rest are observables of the current state, all
+ * accumulated in double on the device. */
+typedef struct ppf_stats {
+    double sum_dc2;       /* sum dc^2 of the last step ("c=" in :240) */
+    double sum_detaS2;    /* sum detaS^2 ("S=") */
+    double sum_detaL2;    /* sum detaL^2 ("L=") */
+    double mass;          /* sum c (total solute, cell volume dx^3 not applied) */
+    double solid;         /* sum hS, the solid phase fraction times cells */
+    double solid_cells;   /* number of cells with etaS > 0.5 */
+    double free_energy;   /* sum of the free-energy density times dx^3 */
+    int64_t cells;        /* nz*ny*nx */
+    int64_t nonfinite;    /* cells holding a NaN/Inf in any field */
+    int64_t steps;        /* steps taken by this context since ppf_upload */
+} ppf_stats;
+
+typedef struct ppf_ctx ppf_ctx;
+
+/* The reference's constants (phasefield.c:76-97). */
+void ppf_params_default(ppf_params *p);
+
+/* Derived constants exactly as phasefield.c:85-97 computes them. */
+int ppf_params_derive(const ppf_params *p, ppf_derived *d);
+
+/* Create a context for an nz x ny x nx interior grid on the current CUDA
+ * device.  Replaces the global arrays of phasefield.c:67-70 and the
+ * compile-time grid/BC macros of :13-56.  `bc` is PPF_BC_*; `precision`
+ * is PPF_F64 or PPF_F32. */
+int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, int precision,
+               ppf_ctx **out);
+int ppf_destroy(ppf_ctx *ctx);
+
+/* Grid and layout of a context. */
+int ppf_get_dims(const ppf_ctx *ctx, int *nz, int *ny, int *nx);
+
+/* Use the caller's CUDA stream (a cudaStream_t) for all later work;
+ * NULL returns to the context's own stream. */
+int ppf_set_stream(ppf_ctx *ctx, void *stream);
+
+/* Host <-> device copies of the interior, replacing read_hdf5's fill of
+ * the ghosted arrays (phasefield.c:996-1049) and the write-out of
+ * write_hdf5 (:1052-1109).  Host arrays may be pageable or pinned.  The
+ * ghost layers are filled on upload (the BC fill of :207-211). */
+int ppf_upload(ppf_ctx *ctx, const double *etaS, const double *etaL, const double *c);
+int ppf_download(ppf_ctx *ctx, double *etaS, double *etaL, double *c);
+
+/* Same, from/to device memory (nz*ny*nx doubles each, C order). */
+int ppf_upload_device(ppf_ctx *ctx, const double *etaS, const double *etaL, const double *c);
+int ppf_download_device(ppf_ctx *ctx, double *etaS, double *etaL, double *c);
+
+/* Advance `nsteps` full steps: for each, the BC fill (:207-211) followed by
+ * sweep_fields (:301-403), fused into one kernel per step.  The increments
+ * of the last step are reduced for ppf_reduce's sum_* fields. */
+int ppf_step(ppf_ctx *ctx, int64_t nsteps);
+
+/* Advance `nsteps` c-only steps: BC fill + sweep_fields_c (:406-476). */
+int ppf_step_c_only(ppf_ctx *ctx, int64_t nsteps);
+
+/* Reductions of the current state plus the last step's increments. */
+int ppf_reduce(ppf_ctx *ctx, ppf_stats *out);
+
+/* Wait for all work queued on the context's stream. */
+int ppf_sync(ppf_ctx *ctx);
+
+/* Message for the calling thread's last failure ("" if none). */
+const char *ppf_last_error(void);
+
+/* Library version string. */
+const char *ppf_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PPF_H */

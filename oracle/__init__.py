@@ -1,0 +1,91 @@
+"""ORACLE -- test infrastructure, not product code.
+
+ctypes access to the CPU restatement of the reference step
+(oracle/ppf_oracle.c, built into oracle/_build/libppf_oracle.so) and to the
+patched reference build recipe (oracle/build_ref.py).  Only tests/, the
+smoke check and bench.py's CPU baseline import this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libppf_oracle.so")
+
+_PARAM_FIELDS = ("AS", "AL", "CS", "CL", "cS0", "cL0", "cSeq", "cLeq", "DL", "DS", "sigma", "gamma", "dx", "dt", "l")
+
+
+class Params(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in _PARAM_FIELDS]
+
+
+class Derived(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("ML", "MS", "h2", "dt", "l", "m", "kappa", "L", "dt_limit")]
+
+
+def reference_params(**over) -> Params:
+    """phasefield.c:76-97 (dt=0 / l=0 select the reference's formulas)."""
+    v = dict(AS=1e9, AL=1e9, CS=-1e6, CL=1e7, cS0=0.455, cL0=0.978, cSeq=0.999, cLeq=0.476, DL=1e-14, DS=0.0,
+             sigma=2.0, gamma=1.5, dx=1.0, dt=0.0, l=0.0)
+    v.update(over)
+    return Params(*[float(v[n]) for n in _PARAM_FIELDS])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} missing: run phasefield_coarsening_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        L.ppf_oracle_run.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64,
+                                                          ctypes.c_int64] + [ctypes.c_void_p] * 4
+        L.ppf_oracle_observe.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 4
+        L.ppf_oracle_derive.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.ppf_oracle_derive.restype = None
+        _lib = L
+    return _lib
+
+
+def _as_params(p):
+    if p is None:
+        return reference_params()
+    if isinstance(p, Params):
+        return p
+    return Params(*[float(getattr(p, n)) for n in _PARAM_FIELDS])
+
+
+def derive(p=None) -> dict:
+    d = Derived()
+    lib().ppf_oracle_derive(ctypes.byref(_as_params(p)), ctypes.byref(d))
+    return {n: getattr(d, n) for n, _ in d._fields_}
+
+
+def run(etaS, etaL, c, nsteps, bc=0, params=None, n_iter_init=1 << 62):
+    """nsteps iterations of the reference loop body; returns (etaS, etaL, c, sums)."""
+    a = [np.array(x, dtype=np.float64, order="C", copy=True) for x in (etaS, etaL, c)]
+    nz, ny, nx = a[0].shape
+    sums = np.zeros(3)
+    p = _as_params(params)
+    rc = lib().ppf_oracle_run(nz, ny, nx, ctypes.byref(p), int(bc), int(nsteps), int(n_iter_init),
+                              *[x.ctypes.data for x in a], sums.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"oracle run failed ({rc})")
+    return a[0], a[1], a[2], sums
+
+
+def observe(etaS, etaL, c, bc=0, params=None) -> dict:
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (etaS, etaL, c)]
+    nz, ny, nx = a[0].shape
+    out = np.zeros(5)
+    p = _as_params(params)
+    rc = lib().ppf_oracle_observe(nz, ny, nx, ctypes.byref(p), int(bc), *[x.ctypes.data for x in a],
+                                  out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"oracle observe failed ({rc})")
+    return {"mass": out[0], "solid": out[1], "solid_cells": out[2], "free_energy": out[3], "nonfinite": out[4]}

@@ -1,0 +1,243 @@
+"""ppf-gb300: the explicit Moelans multi-phase-field / KKS solute step of
+jijn/phasefield_coarsening (phasefield.c:301-476) on NVIDIA GB300.
+
+The product is the C-ABI library built from ``csrc/`` (``include/ppf.h``,
+``include/ppf_h5.h``) and the ``ppf`` program.  This module is a thin
+ctypes mirror of that boundary for Python callers and tests: it loads the
+in-tree ``_build/libppf_gb300.so`` and fails loudly when it is missing.
+There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libppf_gb300.so")
+EXE_PATH = os.path.join(_PKG, "_build", "ppf")
+
+BC_PERIODIC, BC_NOFLUX = 0, 1
+F64, F32 = 0, 1
+_BC = {"periodic": BC_PERIODIC, "noflux": BC_NOFLUX, BC_PERIODIC: BC_PERIODIC, BC_NOFLUX: BC_NOFLUX}
+_PREC = {"f64": F64, "f32": F32, F64: F64, F32: F32}
+
+EXPORTS = (
+    "ppf_params_default", "ppf_params_derive", "ppf_create", "ppf_destroy", "ppf_get_dims", "ppf_set_stream",
+    "ppf_upload", "ppf_download", "ppf_upload_device", "ppf_download_device", "ppf_step", "ppf_step_c_only",
+    "ppf_reduce", "ppf_sync", "ppf_last_error", "ppf_version",
+    "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_last_error",
+)
+
+_PARAM_FIELDS = ("AS", "AL", "CS", "CL", "cS0", "cL0", "cSeq", "cLeq", "DL", "DS", "sigma", "gamma", "dx", "dt", "l")
+
+
+class Params(ctypes.Structure):
+    """ppf_params: the constants of phasefield.c:76-97."""
+    _fields_ = [(n, ctypes.c_double) for n in _PARAM_FIELDS]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n in _PARAM_FIELDS}
+
+
+class Derived(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("ML", "MS", "h2", "dt", "l", "m", "kappa", "L", "dt_limit")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("sum_dc2", ctypes.c_double), ("sum_detaS2", ctypes.c_double), ("sum_detaL2", ctypes.c_double),
+                ("mass", ctypes.c_double), ("solid", ctypes.c_double), ("solid_cells", ctypes.c_double),
+                ("free_energy", ctypes.c_double), ("cells", ctypes.c_int64), ("nonfinite", ctypes.c_int64),
+                ("steps", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class PPFError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"ppf error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded C-ABI library (built by ``build.build()``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with phasefield_coarsening_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        L.ppf_last_error.restype = ctypes.c_char_p
+        L.ppf_version.restype = ctypes.c_char_p
+        L.ppf_h5_last_error.restype = ctypes.c_char_p
+        L.ppf_params_default.restype = None
+        L.ppf_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Params), ctypes.c_int,
+                                 ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        for n in ("ppf_destroy", "ppf_sync"):
+            getattr(L, n).argtypes = [ctypes.c_void_p]
+        L.ppf_set_stream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        for n in ("ppf_upload", "ppf_download", "ppf_upload_device", "ppf_download_device"):
+            getattr(L, n).argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        for n in ("ppf_step", "ppf_step_c_only"):
+            getattr(L, n).argtypes = [ctypes.c_void_p, ctypes.c_int64]
+        L.ppf_reduce.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
+        L.ppf_get_dims.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 3
+        L.ppf_h5_dims.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
+        L.ppf_h5_read3d.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _dp,
+                                    ctypes.c_int64]
+        L.ppf_h5_write3d.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                     ctypes.POINTER(_dp), ctypes.POINTER(ctypes.c_int64), ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_int64)]
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise PPFError(rc, lib().ppf_last_error().decode(errors="replace"))
+
+
+def params_default(**overrides) -> Params:
+    p = Params()
+    lib().ppf_params_default(ctypes.byref(p))
+    for k, v in overrides.items():
+        setattr(p, k, float(v))
+    return p
+
+
+def derive(p: Params | None = None) -> Derived:
+    p = p if p is not None else params_default()
+    d = Derived()
+    _check(lib().ppf_params_derive(ctypes.byref(p), ctypes.byref(d)))
+    return d
+
+
+def _c64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Simulation:
+    """Host-side mirror of a ppf_ctx (include/ppf.h): one grid, three
+    fields, stepped on the current CUDA device."""
+
+    def __init__(self, shape, params: Params | None = None, bc="periodic", precision="f64"):
+        nz, ny, nx = (int(s) for s in shape)
+        self.shape = (nz, ny, nx)
+        self.params = params if params is not None else params_default()
+        self.bc = _BC[bc]
+        self.precision = _PREC[precision]
+        h = ctypes.c_void_p()
+        _check(lib().ppf_create(nz, ny, nx, ctypes.byref(self.params), self.bc, self.precision, ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ppf_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream_ptr: int | None):
+        _check(lib().ppf_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def upload(self, etaS, etaL, c):
+        a = [_c64(x) for x in (etaS, etaL, c)]
+        for x in a:
+            if x.shape != self.shape:
+                raise ValueError(f"field shape {x.shape} != grid {self.shape}")
+        _check(lib().ppf_upload(self._h, *[x.ctypes.data for x in a]))
+
+    def upload_device(self, ptrs):
+        _check(lib().ppf_upload_device(self._h, *[ctypes.c_void_p(int(p)) for p in ptrs]))
+
+    def download(self):
+        out = [np.empty(self.shape, np.float64) for _ in range(3)]
+        _check(lib().ppf_download(self._h, *[x.ctypes.data for x in out]))
+        return tuple(out)
+
+    def download_into(self, etaS, etaL, c):
+        _check(lib().ppf_download(self._h, *[ctypes.c_void_p(int(p)) for p in (etaS, etaL, c)]))
+
+    def upload_from(self, etaS, etaL, c):
+        """Upload from raw host pointers (e.g. pinned buffers)."""
+        _check(lib().ppf_upload(self._h, *[ctypes.c_void_p(int(p)) for p in (etaS, etaL, c)]))
+
+    def step(self, n: int = 1):
+        _check(lib().ppf_step(self._h, int(n)))
+
+    def step_c_only(self, n: int = 1):
+        _check(lib().ppf_step_c_only(self._h, int(n)))
+
+    def sync(self):
+        _check(lib().ppf_sync(self._h))
+
+    def reduce(self) -> dict:
+        s = Stats()
+        _check(lib().ppf_reduce(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+
+# ---------------------------------------------------------------- HDF5 ----
+
+def h5_dims(path: str, name: str):
+    d = (ctypes.c_int64 * 3)()
+    rc = lib().ppf_h5_dims(path.encode(), name.encode(), d)
+    if rc != 0:
+        raise PPFError(rc, lib().ppf_h5_last_error().decode())
+    return tuple(d)
+
+
+def h5_read(path: str, name: str) -> np.ndarray:
+    dims = h5_dims(path, name)
+    out = np.empty(dims, np.float64)
+    d = (ctypes.c_int64 * 3)()
+    rc = lib().ppf_h5_read3d(path.encode(), name.encode(), d, out.ctypes.data_as(_dp), out.size)
+    if rc != 0:
+        raise PPFError(rc, lib().ppf_h5_last_error().decode())
+    return out
+
+
+def h5_write(path: str, fields: dict, dtype="f64", chunk=None):
+    names = list(fields)
+    arrs = [_c64(fields[n]) for n in names]
+    shape = arrs[0].shape
+    if any(a.shape != shape or a.ndim != 3 for a in arrs):
+        raise ValueError("all datasets must be rank-3 and of one shape")
+    cn = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+    cp = (_dp * len(arrs))(*[a.ctypes.data_as(_dp) for a in arrs])
+    dims = (ctypes.c_int64 * 3)(*shape)
+    ch = (ctypes.c_int64 * 3)(*chunk) if chunk is not None else None
+    rc = lib().ppf_h5_write3d(path.encode(), len(names), cn, cp, dims, 0 if dtype == "f64" else 1, ch)
+    if rc != 0:
+        raise PPFError(rc, lib().ppf_h5_last_error().decode())
+
+
+def read_fields(path: str):
+    return tuple(h5_read(path, n) for n in ("/etaS", "/etaL", "/c"))
+
+
+def write_fields(path: str, etaS, etaL, c, dtype="f64", chunk=None):
+    h5_write(path, {"etaS": etaS, "etaL": etaL, "c": c}, dtype=dtype, chunk=chunk)
+
+
+__all__ = ["Simulation", "Params", "Stats", "Derived", "PPFError", "params_default", "derive", "lib",
+           "h5_read", "h5_write", "h5_dims", "read_fields", "write_fields", "BC_PERIODIC", "BC_NOFLUX",
+           "F64", "F32", "LIB_PATH", "EXE_PATH", "EXPORTS"]

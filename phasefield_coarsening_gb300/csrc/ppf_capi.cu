@@ -1,0 +1,388 @@
+// ppf_capi.cu -- the extern "C" boundary declared in include/ppf.h.
+//
+// A context replaces the reference's global state (phasefield.c:67-70,
+// ten ghosted double arrays) with two ping-pong copies of the three
+// evolving fields in device memory; hS, mu and M are never stored (the
+// fused step recomputes them per plane in shared memory) and the
+// increments detaS/detaL/dc are never stored either (only their squared
+// sums, phasefield.c:228-238, are kept for the convergence test).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "ppf.h"
+#include "ppf_internal.h"
+
+using namespace ppf;
+
+static thread_local char g_err[512];
+
+static int seterr(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CU(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return seterr(PPF_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+struct ppf_ctx {
+    int nz, ny, nx, bc, prec;
+    ppf_params p;
+    ppf_derived d;
+    Geom g;
+    int dev, num_sms;
+    cudaStream_t own, stream;
+    void *state;          // one allocation: 2 buffers x 3 fields x g.total elements
+    void *fld[2][3];      // [buffer][etaS, etaL, c]
+    int cur_eta, cur_c;   // buffer holding the current eta / c
+    double *staging;      // 3 * cells doubles, compact [z][y][x]
+    double *partials;     // per-CTA partial sums
+    int partials_cap;     // in doubles
+    double *dres;         // device results: [0..2] increments, [3..7] observables
+    int zc;
+    int64_t steps;
+    int uploaded;
+    Coef<float> kf;
+    Coef<double> kd;
+    CoefD cd;
+};
+
+extern "C" void ppf_params_default(ppf_params *p) {
+    if (!p) return;
+    // phasefield.c:76-97
+    p->AS = 1e+09;
+    p->AL = 1e+09;
+    p->CS = -1e+06;
+    p->CL = 1.e+07;
+    p->cS0 = 0.455;
+    p->cL0 = 0.978;
+    p->cSeq = 0.999;
+    p->cLeq = 0.476;
+    p->DL = 1.0e-14;
+    p->DS = 0.0;
+    p->sigma = 2.0;
+    p->gamma = 1.5;
+    p->dx = 1;
+    p->dt = 0;   // 0.125*dx*dx/DL
+    p->l = 0;    // 7*dx
+}
+
+extern "C" int ppf_params_derive(const ppf_params *p, ppf_derived *d) {
+    if (!p || !d) return seterr(PPF_EINVAL, "null argument");
+    if (!(p->dx > 0) || !(p->AS > 0) || !(p->AL > 0) || !(p->DL > 0) || p->DS < 0 || !(p->sigma > 0) ||
+        p->cSeq == p->cLeq)
+        return seterr(PPF_EINVAL, "invalid parameters (need dx, AS, AL, DL, sigma > 0, DS >= 0, cSeq != cLeq)");
+    d->ML = p->DL / p->AL;                              // :85
+    d->MS = p->DS / p->AS;
+    d->h2 = 1.0 / (p->dx * p->dx);                      // :91
+    d->dt = p->dt > 0 ? p->dt : 0.125 * p->dx * p->dx / p->DL;   // :92
+    d->l = p->l > 0 ? p->l : 7.0 * p->dx;              // :94
+    d->m = 6.0 * p->sigma / d->l;                       // :95
+    d->kappa = 3 * 0.25 * p->sigma * d->l;              // :96
+    d->L = 4.0 / 3.0 * d->m / d->kappa *
+           (0.5 * (d->MS + d->ML) / ((p->cSeq - p->cLeq) * (p->cSeq - p->cLeq)));   // :97
+    const double D = p->DL > p->DS ? p->DL : p->DS;
+    d->dt_limit = p->dx * p->dx / (6.0 * D);
+    return PPF_OK;
+}
+
+template <typename T>
+static Coef<T> make_coef(const ppf_params &p, const ppf_derived &d) {
+    Coef<T> k;
+    k.AS = (T)p.AS;
+    k.AL = (T)p.AL;
+    k.dA = (T)(p.AL - p.AS);
+    k.AsAl = (T)(p.AS * p.AL);
+    k.cS0 = (T)p.cS0;
+    k.cL0 = (T)p.cL0;
+    k.dc0 = (T)(p.cL0 - p.cS0);
+    k.CS = (T)p.CS;
+    k.CL = (T)p.CL;
+    k.halfAS = (T)(0.5 * p.AS);
+    k.halfAL = (T)(0.5 * p.AL);
+    k.ML = (T)d.ML;
+    k.dM = (T)(d.MS - d.ML);
+    k.tmp1 = (T)(-1.0 * d.L * d.dt);
+    k.tmp2 = (T)(p.AS * p.cS0 - p.AL * p.cL0);
+    k.tmp3 = (T)(d.dt * 0.5 * d.h2);
+    k.m = (T)d.m;
+    k.twogam = (T)(2.0 * p.gamma);
+    k.kh2 = (T)(d.kappa * d.h2);
+    return k;
+}
+
+static int default_zc(const ppf_ctx *c) {
+    // enough CTAs for ~4 per SM while keeping the z-march long enough that
+    // the two extra halo planes per CTA stay a small overhead
+    const int tx = c->prec == PPF_F32 ? 64 : 32, ty = 8;
+    const int64_t tiles = (int64_t)((c->nx + tx - 1) / tx) * ((c->ny + ty - 1) / ty);
+    const int64_t want = 4LL * c->num_sms;
+    int64_t chunks = (want + tiles - 1) / tiles;
+    if (chunks < 1) chunks = 1;
+    int zc = (int)((c->nz + chunks - 1) / chunks);
+    if (zc < 4) zc = 4;
+    if (zc > c->nz) zc = c->nz;
+    return zc;
+}
+
+static Fields<float> ff(ppf_ctx *c, int be, int bc_) {
+    return {(float *)c->fld[be][0], (float *)c->fld[be][1], (float *)c->fld[bc_][2]};
+}
+static Fields<double> fd(ppf_ctx *c, int be, int bc_) {
+    return {(double *)c->fld[be][0], (double *)c->fld[be][1], (double *)c->fld[bc_][2]};
+}
+template <typename T>
+static Fields<const T> cst(Fields<T> f) {
+    return {f.eS, f.eL, f.c};
+}
+
+static int ensure_partials(ppf_ctx *c, int ndoubles) {
+    if (ndoubles <= c->partials_cap) return PPF_OK;
+    if (c->partials) cudaFree(c->partials);
+    c->partials = nullptr;
+    c->partials_cap = 0;
+    CU(cudaMalloc(&c->partials, (size_t)ndoubles * sizeof(double)));
+    c->partials_cap = ndoubles;
+    return PPF_OK;
+}
+
+extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, int precision, ppf_ctx **out) {
+    if (!out) return seterr(PPF_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (nz < 1 || ny < 1 || nx < 1 || nz > 8192 || ny > 8192 || nx > 8192)
+        return seterr(PPF_EINVAL, "grid %dx%dx%d out of range [1, 8192]", nz, ny, nx);
+    if (bc != PPF_BC_PERIODIC && bc != PPF_BC_NOFLUX) return seterr(PPF_EINVAL, "bad bc %d", bc);
+    if (precision != PPF_F64 && precision != PPF_F32) return seterr(PPF_EINVAL, "bad precision %d", precision);
+    ppf_params prm;
+    if (p) prm = *p;
+    else ppf_params_default(&prm);
+    ppf_derived der;
+    int rc = ppf_params_derive(&prm, &der);
+    if (rc) return rc;
+    int dev = 0, ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev < 1)
+        return seterr(PPF_ECUDA, "no CUDA device: %s", e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+    CU(cudaGetDevice(&dev));
+    ppf_ctx *c = new (std::nothrow) ppf_ctx();
+    if (!c) return seterr(PPF_ENOMEM, "host allocation failed");
+    c->nz = nz; c->ny = ny; c->nx = nx; c->bc = bc; c->prec = precision;
+    c->p = prm;
+    c->d = der;
+    c->dev = dev;
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    c->g = precision == PPF_F32 ? make_geom<float>(nz, ny, nx, bc) : make_geom<double>(nz, ny, nx, bc);
+    c->kf = make_coef<float>(prm, der);
+    c->kd = make_coef<double>(prm, der);
+    c->cd.AS = prm.AS; c->cd.AL = prm.AL; c->cd.dA = prm.AL - prm.AS;
+    c->cd.cS0 = prm.cS0; c->cd.cL0 = prm.cL0; c->cd.CS = prm.CS; c->cd.CL = prm.CL;
+    c->cd.tmp2 = prm.AS * prm.cS0 - prm.AL * prm.cL0;
+    c->cd.m = der.m; c->cd.gamma = prm.gamma; c->cd.kappa_h2_half = 0.5 * der.kappa * der.h2;
+    c->cd.vol = prm.dx * prm.dx * prm.dx;
+    c->zc = default_zc(c);
+    const size_t es = precision == PPF_F32 ? 4 : 8;
+    const size_t fbytes = (size_t)c->g.total * es;
+    const int64_t cells = (int64_t)nz * ny * nx;
+    cudaError_t e1 = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+    cudaError_t e2 = e1 == cudaSuccess ? cudaMalloc(&c->state, 6 * fbytes) : e1;
+    cudaError_t e3 = e2 == cudaSuccess ? cudaMalloc(&c->staging, 3 * (size_t)cells * sizeof(double)) : e2;
+    cudaError_t e4 = e3 == cudaSuccess ? cudaMalloc(&c->dres, 16 * sizeof(double)) : e3;
+    if (e4 != cudaSuccess) {
+        ppf_destroy(c);
+        return seterr(e4 == cudaErrorMemoryAllocation ? PPF_ENOMEM : PPF_ECUDA, "device setup failed: %s",
+                      cudaGetErrorString(e4));
+    }
+    c->stream = c->own;
+    for (int b = 0; b < 2; ++b)
+        for (int f = 0; f < 3; ++f) c->fld[b][f] = (char *)c->state + (size_t)(3 * b + f) * fbytes;
+    // zero the padding once so that unused ghost edges hold finite values
+    e = cudaMemsetAsync(c->state, 0, 6 * fbytes, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dres, 0, 16 * sizeof(double), c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        ppf_destroy(c);
+        return seterr(PPF_ECUDA, "device init failed: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return PPF_OK;
+}
+
+extern "C" int ppf_destroy(ppf_ctx *c) {
+    if (!c) return PPF_OK;
+    if (c->own) cudaStreamSynchronize(c->own);
+    if (c->stream && c->stream != c->own) cudaStreamSynchronize(c->stream);
+    if (c->state) cudaFree(c->state);
+    if (c->staging) cudaFree(c->staging);
+    if (c->partials) cudaFree(c->partials);
+    if (c->dres) cudaFree(c->dres);
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+    return PPF_OK;
+}
+
+extern "C" int ppf_get_dims(const ppf_ctx *c, int *nz, int *ny, int *nx) {
+    if (!c) return seterr(PPF_EINVAL, "null context");
+    if (nz) *nz = c->nz;
+    if (ny) *ny = c->ny;
+    if (nx) *nx = c->nx;
+    return PPF_OK;
+}
+
+extern "C" int ppf_set_stream(ppf_ctx *c, void *stream) {
+    if (!c) return seterr(PPF_EINVAL, "null context");
+    CU(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? (cudaStream_t)stream : c->own;
+    return PPF_OK;
+}
+
+static int do_pack(ppf_ctx *c) {
+    c->cur_eta = 0;
+    c->cur_c = 0;
+    if (c->prec == PPF_F32) CU(launch_pack<float>(c->g, c->staging, ff(c, 0, 0), c->stream));
+    else CU(launch_pack<double>(c->g, c->staging, fd(c, 0, 0), c->stream));
+    CU(cudaMemsetAsync(c->dres, 0, 3 * sizeof(double), c->stream));
+    c->uploaded = 1;
+    c->steps = 0;
+    return PPF_OK;
+}
+
+extern "C" int ppf_upload(ppf_ctx *c, const double *etaS, const double *etaL, const double *cc) {
+    if (!c || !etaS || !etaL || !cc) return seterr(PPF_EINVAL, "null argument");
+    const size_t n = (size_t)c->nz * c->ny * c->nx;
+    CU(cudaMemcpyAsync(c->staging, etaS, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->staging + n, etaL, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->staging + 2 * n, cc, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int rc = do_pack(c);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    return PPF_OK;
+}
+
+extern "C" int ppf_upload_device(ppf_ctx *c, const double *etaS, const double *etaL, const double *cc) {
+    if (!c || !etaS || !etaL || !cc) return seterr(PPF_EINVAL, "null argument");
+    const size_t n = (size_t)c->nz * c->ny * c->nx;
+    CU(cudaMemcpyAsync(c->staging, etaS, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->staging + n, etaL, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->staging + 2 * n, cc, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    int rc = do_pack(c);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    return PPF_OK;
+}
+
+static int do_unpack(ppf_ctx *c) {
+    if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
+    if (c->prec == PPF_F32)
+        CU(launch_unpack<float>(c->g, cst(ff(c, c->cur_eta, c->cur_c)), c->staging, c->stream));
+    else
+        CU(launch_unpack<double>(c->g, cst(fd(c, c->cur_eta, c->cur_c)), c->staging, c->stream));
+    return PPF_OK;
+}
+
+extern "C" int ppf_download(ppf_ctx *c, double *etaS, double *etaL, double *cc) {
+    if (!c || !etaS || !etaL || !cc) return seterr(PPF_EINVAL, "null argument");
+    int rc = do_unpack(c);
+    if (rc) return rc;
+    const size_t n = (size_t)c->nz * c->ny * c->nx;
+    CU(cudaMemcpyAsync(etaS, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(etaL, c->staging + n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(cc, c->staging + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return PPF_OK;
+}
+
+extern "C" int ppf_download_device(ppf_ctx *c, double *etaS, double *etaL, double *cc) {
+    if (!c || !etaS || !etaL || !cc) return seterr(PPF_EINVAL, "null argument");
+    int rc = do_unpack(c);
+    if (rc) return rc;
+    const size_t n = (size_t)c->nz * c->ny * c->nx;
+    CU(cudaMemcpyAsync(etaS, c->staging, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(etaL, c->staging + n, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(cc, c->staging + 2 * n, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return PPF_OK;
+}
+
+static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
+    if (!c) return seterr(PPF_EINVAL, "null context");
+    if (nsteps < 0) return seterr(PPF_EINVAL, "negative step count");
+    if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
+    if (nsteps == 0) return PPF_OK;
+    const int nb = c->prec == PPF_F32 ? step_blocks<float>(c->g, c->zc) : step_blocks<double>(c->g, c->zc);
+    int rc = ensure_partials(c, 5 * nb > 3 * nb ? 5 * nb : 3 * nb);
+    if (rc) return rc;
+    for (int64_t s = 0; s < nsteps; ++s) {
+        const bool last = s == nsteps - 1;
+        const int ie = c->cur_eta, ic = c->cur_c;
+        const int oe = c_only ? ie : 1 - ie, oc = 1 - ic;
+        double *part = last ? c->partials : nullptr;
+        cudaError_t e;
+        if (c->prec == PPF_F32)
+            e = launch_step<float>(c->g, c->kf, cst(ff(c, ie, ic)), ff(c, oe, oc), c_only, part, c->zc, c->stream,
+                                   nullptr);
+        else
+            e = launch_step<double>(c->g, c->kd, cst(fd(c, ie, ic)), fd(c, oe, oc), c_only, part, c->zc, c->stream,
+                                    nullptr);
+        if (e != cudaSuccess) return seterr(PPF_ECUDA, "step launch failed: %s", cudaGetErrorString(e));
+        c->cur_eta = oe;
+        c->cur_c = oc;
+        c->steps++;
+        if (last) CU(launch_final_sum(c->partials, nb, 3, c_only ? 1 : 3, c->dres, c->stream));
+    }
+    return PPF_OK;
+}
+
+extern "C" int ppf_step(ppf_ctx *c, int64_t nsteps) { return run_steps(c, nsteps, false); }
+
+extern "C" int ppf_step_c_only(ppf_ctx *c, int64_t nsteps) { return run_steps(c, nsteps, true); }
+
+extern "C" int ppf_reduce(ppf_ctx *c, ppf_stats *out) {
+    if (!c || !out) return seterr(PPF_EINVAL, "null argument");
+    if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
+    const int64_t cells = (int64_t)c->nz * c->ny * c->nx;
+    int nb = (int)((cells + 255) / 256);
+    if (nb > 4 * c->num_sms) nb = 4 * c->num_sms;
+    int rc = ensure_partials(c, 5 * nb);
+    if (rc) return rc;
+    if (c->prec == PPF_F32)
+        CU(launch_observe<float>(c->g, c->cd, cst(ff(c, c->cur_eta, c->cur_c)), c->partials, nb, c->stream));
+    else
+        CU(launch_observe<double>(c->g, c->cd, cst(fd(c, c->cur_eta, c->cur_c)), c->partials, nb, c->stream));
+    CU(launch_final_sum(c->partials, nb, 5, 5, c->dres + 3, c->stream));
+    double h[8];
+    CU(cudaMemcpyAsync(h, c->dres, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    out->sum_dc2 = h[0];
+    out->sum_detaS2 = h[1];
+    out->sum_detaL2 = h[2];
+    out->mass = h[3];
+    out->solid = h[4];
+    out->solid_cells = h[5];
+    out->free_energy = h[6];
+    out->nonfinite = (int64_t)h[7];
+    out->cells = cells;
+    out->steps = c->steps;
+    return PPF_OK;
+}
+
+extern "C" int ppf_sync(ppf_ctx *c) {
+    if (!c) return seterr(PPF_EINVAL, "null context");
+    CU(cudaStreamSynchronize(c->stream));
+    return PPF_OK;
+}
+
+extern "C" const char *ppf_last_error(void) { return g_err; }
+
+extern "C" const char *ppf_version(void) { return "ppf-gb300 0.1 (sm_103a)"; }

@@ -1,0 +1,97 @@
+// ppf_internal.h -- device data layout and kernel launchers shared by the
+// C-ABI translation units.  Not part of the public interface (include/ppf.h).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ppf {
+
+// HBM layout of one field: the reference's ghosted array
+// double[NI+2][NJ+2][NK+2] (phasefield.c:67-70), with the x rows padded so
+// that every row starts on a 32-byte sector and the interior x=0 does too:
+//   storage(x, y, z) = (z+1)*PS + (y+1)*P + xoff + x,   x,y,z in [-1, n]
+// xoff = 32 bytes / sizeof(T); P = row pitch, a multiple of 32 bytes with
+// room for the ghost column x = nx.  Face ghosts hold the boundary
+// condition for the next step; edges and corners are never read.
+struct Geom {
+    int nx, ny, nz;
+    int xoff;
+    int bc;
+    int64_t P, PS, total;
+    __host__ __device__ __forceinline__ int64_t at(int x, int y, int z) const {
+        return (int64_t)(z + 1) * PS + (int64_t)(y + 1) * P + (int64_t)(x + xoff);
+    }
+};
+
+template <typename T>
+Geom make_geom(int nz, int ny, int nx, int bc) {
+    Geom g;
+    g.nx = nx; g.ny = ny; g.nz = nz; g.bc = bc;
+    const int per32 = 32 / (int)sizeof(T);
+    g.xoff = per32;
+    g.P = ((int64_t)(g.xoff + nx + 1) + per32 - 1) / per32 * per32;
+    g.PS = g.P * (ny + 2);
+    g.total = g.PS * (nz + 2);
+    return g;
+}
+
+// Loop-invariant coefficients of sweep_fields (phasefield.c:322-323,
+// :337-339) and of the constants block (:76-97), folded on the host in
+// double and cast once to the step's precision.
+template <typename T>
+struct Coef {
+    T AS, AL, dA, AsAl;       // AS, AL, AL-AS, tmp5 = AS*AL
+    T cS0, cL0, dc0;          // cS0, cL0, tmp6 = cL0-cS0
+    T CS, CL, halfAS, halfAL; // parabola offsets, AS/2, AL/2
+    T ML, dM;                 // ML, MS-ML
+    T tmp1, tmp2, tmp3;       // -L*dt, AS*cS0-AL*cL0, dt*h2/2
+    T m, twogam, kh2;         // m, 2*gamma, kappa*h2
+};
+
+// The same coefficients in double, plus what the observables need.
+struct CoefD {
+    double AS, AL, dA, cS0, cL0, CS, CL, tmp2, m, gamma, kappa_h2_half, vol;
+};
+
+template <typename T>
+struct Fields {
+    T *eS, *eL, *c;
+};
+
+// Launch shape of the fused step: tiles of tx*ty cells in x-y, each CTA
+// marching zc planes in z.
+struct StepShape {
+    int zc;
+};
+
+// Fused BC-fill + sweep_fields (+ sweep_fields_c when c_only) for one step.
+// `partials` (nullable) receives per-CTA sums of dc^2, detaS^2, detaL^2;
+// returns the number of CTAs through *nblocks.
+template <typename T>
+cudaError_t launch_step(const Geom &g, const Coef<T> &k, Fields<const T> in, Fields<T> out,
+                        bool c_only, double *partials, int zc, cudaStream_t s, int *nblocks);
+
+// Number of CTAs launch_step would use.
+template <typename T>
+int step_blocks(const Geom &g, int zc);
+
+// Pack/unpack between compact double arrays [z][y][x] and the padded
+// layout; pack also writes the face ghosts (the BC fill of :207-211).
+template <typename T>
+cudaError_t launch_pack(const Geom &g, const double *src3, Fields<T> dst, cudaStream_t s);
+template <typename T>
+cudaError_t launch_unpack(const Geom &g, Fields<const T> src, double *dst3, cudaStream_t s);
+
+// Observables of a state: per-CTA partial sums of
+// {mass, solid, solid_cells, free energy, nonfinite} into partials[5*b+i].
+template <typename T>
+cudaError_t launch_observe(const Geom &g, const CoefD &k, Fields<const T> f, double *partials,
+                           int nblocks, cudaStream_t s);
+
+// Deterministic final sum: out[i] = sum_b partials[stride*b + i] for
+// i < nvals (fixed order, one CTA).
+cudaError_t launch_final_sum(const double *partials, int nblocks, int stride, int nvals, double *out,
+                             cudaStream_t s);
+
+}  // namespace ppf

@@ -1,0 +1,117 @@
+"""The HDF5 subset (include/ppf_h5.h): round trips, a file written by real
+libhdf5, and the failure modes the reference ignores."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import phasefield_coarsening_gb300 as ppf
+
+
+def _fields(shape, seed=0):
+    rng = np.random.default_rng(seed)
+    return {n: rng.random(shape) for n in ("etaS", "etaL", "c")}
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("chunk", [None, (2, 3, 4), (1, 1, 1), (5, 6, 7)])
+def test_round_trip(tmp_path, dtype, chunk):
+    shape = (5, 6, 7)
+    f = _fields(shape)
+    p = str(tmp_path / "a.h5")
+    ppf.h5_write(p, f, dtype=dtype, chunk=chunk)
+    for n, a in f.items():
+        got = ppf.h5_read(p, "/" + n)
+        ref = a if dtype == "f64" else a.astype(np.float32).astype(np.float64)
+        assert np.array_equal(got, ref)
+        assert ppf.h5_dims(p, n) == shape
+
+
+def test_chunked_multilevel_btree(tmp_path):
+    # 9*8*9 = 648 chunks > 64 per node: a two-level chunk B-tree
+    shape = (9, 8, 9)
+    f = _fields(shape, 3)
+    p = str(tmp_path / "m.h5")
+    ppf.h5_write(p, f, chunk=(1, 1, 1))
+    for n, a in f.items():
+        assert np.array_equal(ppf.h5_read(p, n), a)
+
+
+def test_mpi_layout_chunk_equals_subdomain(tmp_path):
+    # the reference's MPI writer: chunk = subdomain NN/NQ (phasefield.c:577-579)
+    shape = (12, 12, 12)
+    f = _fields(shape, 5)
+    p = str(tmp_path / "mpi.h5")
+    ppf.h5_write(p, f, chunk=(6, 6, 6))
+    for n, a in f.items():
+        assert np.array_equal(ppf.h5_read(p, n), a)
+
+
+def test_file_layout_is_hdf5_superblock_v0(tmp_path):
+    p = str(tmp_path / "s.h5")
+    ppf.h5_write(p, _fields((2, 2, 2)))
+    b = open(p, "rb").read()
+    assert b[:8] == b"\x89HDF\r\n\x1a\n" and b[8] == 0
+    assert int.from_bytes(b[40:48], "little") == len(b)      # end-of-file address
+    for sig in (b"HEAP", b"TREE", b"SNOD"):
+        assert sig in b
+
+
+def _libhdf5_file():
+    try:
+        import scipy
+    except ImportError:
+        return None
+    c = glob.glob(os.path.join(os.path.dirname(scipy.__file__), "io", "matlab", "tests", "data",
+                               "testhdf5_7.4_GLNX86.mat"))
+    return c[0] if c else None
+
+
+def test_reads_structure_of_file_written_by_libhdf5():
+    """A MATLAB v7.3 file (libhdf5, 512-byte user block): the symbol-table
+    walk must find its dataset and report its rank-2 shape as unsupported."""
+    p = _libhdf5_file()
+    if p is None:
+        pytest.skip("scipy test data not installed")
+    with pytest.raises(ppf.PPFError) as e:
+        ppf.h5_dims(p, "testdouble")
+    assert e.value.code == -4 and "rank 2" in str(e.value)
+    with pytest.raises(ppf.PPFError) as e:
+        ppf.h5_dims(p, "nosuch")
+    assert e.value.code == -3
+
+
+def test_errors(tmp_path):
+    p = str(tmp_path / "e.h5")
+    ppf.h5_write(p, _fields((3, 3, 3)))
+    with pytest.raises(ppf.PPFError) as e:
+        ppf.h5_read(p, "/missing")
+    assert e.value.code == -3
+    with pytest.raises(ppf.PPFError) as e:
+        ppf.h5_read(str(tmp_path / "none.h5"), "/etaS")
+    assert e.value.code == -1
+    bad = tmp_path / "bad.h5"
+    bad.write_bytes(b"not an hdf5 file at all" * 10)
+    with pytest.raises(ppf.PPFError) as e:
+        ppf.h5_read(str(bad), "/etaS")
+    assert e.value.code == -2
+    # truncated: the data block is cut off
+    raw = open(p, "rb").read()
+    tr = tmp_path / "trunc.h5"
+    tr.write_bytes(raw[: len(raw) - 100])
+    for name in ("/etaS", "/c"):
+        with pytest.raises(ppf.PPFError) as e:
+            ppf.h5_read(str(tr), name)
+        assert e.value.code == -1 and "truncated" in str(e.value)
+
+
+def test_user_block_is_skipped(tmp_path):
+    p = str(tmp_path / "u.h5")
+    f = _fields((3, 4, 5), 9)
+    ppf.h5_write(p, f)
+    raw = open(p, "rb").read()
+    # prepend a 512-byte user block; addresses are relative to the superblock
+    ub = tmp_path / "ub.h5"
+    ub.write_bytes(b"\0" * 512 + raw)
+    assert np.array_equal(ppf.h5_read(str(ub), "etaS"), f["etaS"])

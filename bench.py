@@ -68,7 +68,7 @@ class ClockSampler:
             os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -169,7 +169,9 @@ def run_ours(args):
     shape = eS.shape
     cells = int(np.prod(shape))
     sim = ppf.Simulation(shape, ppf.params_default(dt=DT), bc="periodic", precision="f32")
-    stream = torch.cuda.current_stream()
+    # a real (non-NULL) stream shared by the kernels and the timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sim.set_stream(stream.cuda_stream)
     sim.upload(eS, eL, c)
 
@@ -177,13 +179,13 @@ def run_ours(args):
         sim.step(INNER)
         return sim.reduce()
 
+    clocks = ClockSampler(local)
+    clocks.start()
     for _ in range(args.warmup):
         bench_step()
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
@@ -317,7 +319,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--seed", type=int, default=0)

@@ -23,9 +23,10 @@
  *   - every function returns 0 on success or a negative PPF_E* code;
  *     ppf_last_error() returns a message for the calling thread's last
  *     failure;
- *   - calls on one context are synchronous with respect to the host unless
- *     the name says _async; one context must not be used from two threads
- *     at once; contexts are independent of each other;
+ *   - ppf_step / ppf_step_c_only queue work on the context's stream and
+ *     return; ppf_upload*, ppf_download*, ppf_reduce and ppf_sync wait for
+ *     it (errors of queued work surface there); one context must not be
+ *     used from two threads at once; contexts are independent;
  *   - nothing here falls back to the CPU: without a usable CUDA device
  *     ppf_create fails with PPF_ECUDA.
  */
@@ -144,8 +145,22 @@ int ppf_step_c_only(ppf_ctx *ctx, int64_t nsteps);
 /* Reductions of the current state plus the last step's increments. */
 int ppf_reduce(ppf_ctx *ctx, ppf_stats *out);
 
-/* Wait for all work queued on the context's stream. */
+/* Wait for all work queued on the context's stream.  Returns
+ * PPF_ETIMEOUT when a step's bounded device wait ran out since the last
+ * check (the state of that step is then invalid: upload a new one). */
 int ppf_sync(ppf_ctx *ctx);
+
+/* Upper bound, in seconds, of every device-side wait of the step kernel
+ * (default 1 s).  No counterpart in the reference. */
+int ppf_set_wait_limit(ppf_ctx *ctx, double seconds);
+
+/* Test hook, no counterpart in the reference: make the next step's kernel
+ * wait on a copy that never completes, so that the wait limit runs out and
+ * the failure path (error word, PPF_ETIMEOUT, usable context) can be
+ * exercised without faulting the GPU. */
+#define PPF_INJECT_NONE       0
+#define PPF_INJECT_STALL_WAIT 1
+int ppf_debug_inject(ppf_ctx *ctx, int fault);
 
 /* Message for the calling thread's last failure ("" if none). */
 const char *ppf_last_error(void);

@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(_PKG, "_build", "libppf_gb300.so")
 EXE_PATH = os.path.join(_PKG, "_build", "ppf")
 
 BC_PERIODIC, BC_NOFLUX = 0, 1
+INJECT_NONE, INJECT_STALL_WAIT = 0, 1
 F64, F32 = 0, 1
 _BC = {"periodic": BC_PERIODIC, "noflux": BC_NOFLUX, BC_PERIODIC: BC_PERIODIC, BC_NOFLUX: BC_NOFLUX}
 _PREC = {"f64": F64, "f32": F32, F64: F64, F32: F32}
@@ -26,7 +27,7 @@ _PREC = {"f64": F64, "f32": F32, F64: F64, F32: F32}
 EXPORTS = (
     "ppf_params_default", "ppf_params_derive", "ppf_create", "ppf_destroy", "ppf_get_dims", "ppf_set_stream",
     "ppf_upload", "ppf_download", "ppf_upload_device", "ppf_download_device", "ppf_step", "ppf_step_c_only",
-    "ppf_reduce", "ppf_sync", "ppf_last_error", "ppf_version",
+    "ppf_reduce", "ppf_sync", "ppf_set_wait_limit", "ppf_debug_inject", "ppf_last_error", "ppf_version",
     "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_last_error",
 )
 
@@ -89,6 +90,8 @@ def lib() -> ctypes.CDLL:
         for n in ("ppf_step", "ppf_step_c_only"):
             getattr(L, n).argtypes = [ctypes.c_void_p, ctypes.c_int64]
         L.ppf_reduce.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
+        L.ppf_set_wait_limit.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.ppf_debug_inject.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.ppf_get_dims.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 3
         L.ppf_h5_dims.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.ppf_h5_read3d.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _dp,
@@ -188,6 +191,12 @@ class Simulation:
 
     def sync(self):
         _check(lib().ppf_sync(self._h))
+
+    def set_wait_limit(self, seconds: float):
+        _check(lib().ppf_set_wait_limit(self._h, float(seconds)))
+
+    def debug_inject(self, fault: int):
+        _check(lib().ppf_debug_inject(self._h, int(fault)))
 
     def reduce(self) -> dict:
         s = Stats()

@@ -17,6 +17,7 @@
 
 #include "ppf.h"
 #include "ppf_internal.h"
+#include "ppf_step_tma.h"
 
 using namespace ppf;
 
@@ -51,7 +52,11 @@ struct ppf_ctx {
     double *partials;     // per-CTA partial sums
     int partials_cap;     // in doubles
     double *dres;         // device results: [0..2] increments, [3..7] observables
-    int zc;
+    int *derr;            // device error word set by a kernel whose bounded wait ran out
+    CUtensorMap maps[2][3];   // TMA maps of the fields of both buffers
+    int grid;             // persistent grid of the fused step
+    unsigned long long wait_limit_ns;
+    int inject;           // test hook: PPF_INJECT_*
     int64_t steps;
     int uploaded;
     Coef<float> kf;
@@ -123,19 +128,7 @@ static Coef<T> make_coef(const ppf_params &p, const ppf_derived &d) {
     return k;
 }
 
-static int default_zc(const ppf_ctx *c) {
-    // enough CTAs for ~4 per SM while keeping the z-march long enough that
-    // the two extra halo planes per CTA stay a small overhead
-    const int tx = c->prec == PPF_F32 ? 64 : 32, ty = 8;
-    const int64_t tiles = (int64_t)((c->nx + tx - 1) / tx) * ((c->ny + ty - 1) / ty);
-    const int64_t want = 4LL * c->num_sms;
-    int64_t chunks = (want + tiles - 1) / tiles;
-    if (chunks < 1) chunks = 1;
-    int zc = (int)((c->nz + chunks - 1) / chunks);
-    if (zc < 4) zc = 4;
-    if (zc > c->nz) zc = c->nz;
-    return zc;
-}
+static int check_device_error(ppf_ctx *c);
 
 static Fields<float> ff(ppf_ctx *c, int be, int bc_) {
     return {(float *)c->fld[be][0], (float *)c->fld[be][1], (float *)c->fld[bc_][2]};
@@ -191,25 +184,40 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
     c->cd.tmp2 = prm.AS * prm.cS0 - prm.AL * prm.cL0;
     c->cd.m = der.m; c->cd.gamma = prm.gamma; c->cd.kappa_h2_half = 0.5 * der.kappa * der.h2;
     c->cd.vol = prm.dx * prm.dx * prm.dx;
-    c->zc = default_zc(c);
     const size_t es = precision == PPF_F32 ? 4 : 8;
     const size_t fbytes = (size_t)c->g.total * es;
     const int64_t cells = (int64_t)nz * ny * nx;
     cudaError_t e1 = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
     cudaError_t e2 = e1 == cudaSuccess ? cudaMalloc(&c->state, 6 * fbytes) : e1;
     cudaError_t e3 = e2 == cudaSuccess ? cudaMalloc(&c->staging, 3 * (size_t)cells * sizeof(double)) : e2;
-    cudaError_t e4 = e3 == cudaSuccess ? cudaMalloc(&c->dres, 16 * sizeof(double)) : e3;
+    cudaError_t e4 = e3 == cudaSuccess ? cudaMalloc(&c->dres, 16 * sizeof(double) + 64) : e3;
     if (e4 != cudaSuccess) {
         ppf_destroy(c);
         return seterr(e4 == cudaErrorMemoryAllocation ? PPF_ENOMEM : PPF_ECUDA, "device setup failed: %s",
                       cudaGetErrorString(e4));
     }
     c->stream = c->own;
+    c->derr = (int *)(c->dres + 16);
+    c->wait_limit_ns = 1000000000ULL;
     for (int b = 0; b < 2; ++b)
         for (int f = 0; f < 3; ++f) c->fld[b][f] = (char *)c->state + (size_t)(3 * b + f) * fbytes;
+    for (int b = 0; b < 2 && rc == PPF_OK; ++b)
+        for (int f = 0; f < 3; ++f) {
+            int mr = precision == PPF_F32 ? make_field_map<float>(c->g, (const float *)c->fld[b][f], &c->maps[b][f])
+                                          : make_field_map<double>(c->g, (const double *)c->fld[b][f], &c->maps[b][f]);
+            if (mr != 0) {
+                ppf_destroy(c);
+                return seterr(PPF_ECUDA, "TMA descriptor setup failed (%d)", mr);
+            }
+        }
+    c->grid = precision == PPF_F32 ? tma_grid<float>(c->g, c->num_sms) : tma_grid<double>(c->g, c->num_sms);
+    if (c->grid < 1) {
+        ppf_destroy(c);
+        return seterr(PPF_ECUDA, "kernel attribute setup failed");
+    }
     // zero the padding once so that unused ghost edges hold finite values
     e = cudaMemsetAsync(c->state, 0, 6 * fbytes, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->dres, 0, 16 * sizeof(double), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dres, 0, 16 * sizeof(double) + 64, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
         ppf_destroy(c);
@@ -300,7 +308,7 @@ extern "C" int ppf_download(ppf_ctx *c, double *etaS, double *etaL, double *cc) 
     CU(cudaMemcpyAsync(etaL, c->staging + n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaMemcpyAsync(cc, c->staging + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
-    return PPF_OK;
+    return check_device_error(c);
 }
 
 extern "C" int ppf_download_device(ppf_ctx *c, double *etaS, double *etaL, double *cc) {
@@ -315,31 +323,49 @@ extern "C" int ppf_download_device(ppf_ctx *c, double *etaS, double *etaL, doubl
     return PPF_OK;
 }
 
+// Reads and clears the device error word; PPF_ETIMEOUT when a kernel's
+// bounded wait ran out since the last check.
+static int check_device_error(ppf_ctx *c) {
+    int h = 0;
+    CU(cudaMemcpyAsync(&h, c->derr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    if (h) {
+        CU(cudaMemsetAsync(c->derr, 0, sizeof(int), c->stream));
+        CU(cudaStreamSynchronize(c->stream));
+        return seterr(PPF_ETIMEOUT, "a device wait exceeded its limit; the state of that step is invalid");
+    }
+    return PPF_OK;
+}
+
 static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
     if (!c) return seterr(PPF_EINVAL, "null context");
     if (nsteps < 0) return seterr(PPF_EINVAL, "negative step count");
     if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
     if (nsteps == 0) return PPF_OK;
-    const int nb = c->prec == PPF_F32 ? step_blocks<float>(c->g, c->zc) : step_blocks<double>(c->g, c->zc);
-    int rc = ensure_partials(c, 5 * nb > 3 * nb ? 5 * nb : 3 * nb);
+    int rc = ensure_partials(c, 3 * c->grid);
     if (rc) return rc;
     for (int64_t s = 0; s < nsteps; ++s) {
         const bool last = s == nsteps - 1;
         const int ie = c->cur_eta, ic = c->cur_c;
         const int oe = c_only ? ie : 1 - ie, oc = 1 - ic;
         double *part = last ? c->partials : nullptr;
+        const int inject = c->inject;
+        c->inject = PPF_INJECT_NONE;
         cudaError_t e;
-        if (c->prec == PPF_F32)
-            e = launch_step<float>(c->g, c->kf, cst(ff(c, ie, ic)), ff(c, oe, oc), c_only, part, c->zc, c->stream,
-                                   nullptr);
-        else
-            e = launch_step<double>(c->g, c->kd, cst(fd(c, ie, ic)), fd(c, oe, oc), c_only, part, c->zc, c->stream,
-                                    nullptr);
+        if (c->prec == PPF_F32) {
+            const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
+            e = launch_step_tma<float>(c->g, c->kf, m, ff(c, oe, oc), c_only, part, c->grid, c->derr,
+                                       c->wait_limit_ns, inject, c->stream);
+        } else {
+            const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
+            e = launch_step_tma<double>(c->g, c->kd, m, fd(c, oe, oc), c_only, part, c->grid, c->derr,
+                                        c->wait_limit_ns, inject, c->stream);
+        }
         if (e != cudaSuccess) return seterr(PPF_ECUDA, "step launch failed: %s", cudaGetErrorString(e));
         c->cur_eta = oe;
         c->cur_c = oc;
         c->steps++;
-        if (last) CU(launch_final_sum(c->partials, nb, 3, c_only ? 1 : 3, c->dres, c->stream));
+        if (last) CU(launch_final_sum(c->partials, c->grid, 3, c_only ? 1 : 3, c->dres, c->stream));
     }
     return PPF_OK;
 }
@@ -364,6 +390,8 @@ extern "C" int ppf_reduce(ppf_ctx *c, ppf_stats *out) {
     double h[8];
     CU(cudaMemcpyAsync(h, c->dres, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
+    rc = check_device_error(c);
+    if (rc) return rc;
     out->sum_dc2 = h[0];
     out->sum_detaS2 = h[1];
     out->sum_detaL2 = h[2];
@@ -380,6 +408,20 @@ extern "C" int ppf_reduce(ppf_ctx *c, ppf_stats *out) {
 extern "C" int ppf_sync(ppf_ctx *c) {
     if (!c) return seterr(PPF_EINVAL, "null context");
     CU(cudaStreamSynchronize(c->stream));
+    return check_device_error(c);
+}
+
+extern "C" int ppf_set_wait_limit(ppf_ctx *c, double seconds) {
+    if (!c) return seterr(PPF_EINVAL, "null context");
+    if (!(seconds > 0) || seconds > 60) return seterr(PPF_EINVAL, "wait limit must be in (0, 60] s");
+    c->wait_limit_ns = (unsigned long long)(seconds * 1e9);
+    return PPF_OK;
+}
+
+extern "C" int ppf_debug_inject(ppf_ctx *c, int fault) {
+    if (!c) return seterr(PPF_EINVAL, "null context");
+    if (fault != PPF_INJECT_NONE && fault != PPF_INJECT_STALL_WAIT) return seterr(PPF_EINVAL, "unknown fault %d", fault);
+    c->inject = fault;
     return PPF_OK;
 }
 

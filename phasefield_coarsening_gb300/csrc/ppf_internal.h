@@ -59,23 +59,6 @@ struct Fields {
     T *eS, *eL, *c;
 };
 
-// Launch shape of the fused step: tiles of tx*ty cells in x-y, each CTA
-// marching zc planes in z.
-struct StepShape {
-    int zc;
-};
-
-// Fused BC-fill + sweep_fields (+ sweep_fields_c when c_only) for one step.
-// `partials` (nullable) receives per-CTA sums of dc^2, detaS^2, detaL^2;
-// returns the number of CTAs through *nblocks.
-template <typename T>
-cudaError_t launch_step(const Geom &g, const Coef<T> &k, Fields<const T> in, Fields<T> out,
-                        bool c_only, double *partials, int zc, cudaStream_t s, int *nblocks);
-
-// Number of CTAs launch_step would use.
-template <typename T>
-int step_blocks(const Geom &g, int zc);
-
 // Pack/unpack between compact double arrays [z][y][x] and the padded
 // layout; pack also writes the face ghosts (the BC fill of :207-211).
 template <typename T>

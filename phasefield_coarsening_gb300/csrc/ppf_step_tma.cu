@@ -1,0 +1,509 @@
+// ppf_step_tma.cu -- the fused explicit step as a TMA-fed, z-marching,
+// persistent sm_103a kernel.
+//
+// Replaces, per time step, the reference's BC fill (phasefield.c:1112-1189)
+// and the three passes of sweep_fields (:325-335 pass A, :347-391 pass B,
+// :393-401 pass C) -- or of sweep_fields_c (:406-476) in c-only mode.
+//
+// Data flow of one CTA:
+//   * a contiguous range of (x-y tile, z plane) work, balanced over the
+//     persistent grid; each tile column segment is marched up z;
+//   * thread 0 streams every plane's etaS/etaL/c tile plus a one-cell ring
+//     (a TX+2*XH by TY+2 box per field) from HBM into a S-stage shared ring
+//     with cp.async.bulk.tensor.3d, completion signalled on an mbarrier per
+//     stage; S-2 planes are in flight while one is computed;
+//   * pass A (hS, mu, M) is evaluated once per loaded cell into a 3-plane
+//     shared ring of mu/M; each thread owns CY cells stacked in y so that
+//     its y and z neighbours stay in registers;
+//   * pass B + C for plane z-1 then read x/y neighbours from shared memory,
+//     and write the new state straight to HBM, including the face ghosts
+//     the boundary condition defines (so the next step reads ready ghosts).
+// Every mbarrier wait is bounded by a time limit: on expiry the CTA sets an
+// error word, drains its own outstanding copies (again bounded) and exits
+// uniformly; the host reports PPF_ETIMEOUT.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ppf_internal.h"
+#include "ppf_step_tma.h"
+
+namespace ppf {
+
+template <typename T>
+struct TmaCfg;
+template <>
+struct TmaCfg<float> {
+    static constexpr int TX = 64, TY = 16, NT = 256, S = 4, XH = 4;
+};
+template <>
+struct TmaCfg<double> {
+    static constexpr int TX = 32, TY = 16, NT = 256, S = 4, XH = 2;
+};
+
+template <typename T>
+struct TmaGeo {
+    using C = TmaCfg<T>;
+    static constexpr int TX = C::TX, TY = C::TY, NT = C::NT, S = C::S, XH = C::XH;
+    static constexpr int BX = TX + 2 * XH, BY = TY + 2;
+    static constexpr int BOX = BX * BY;                                   // elements per field box
+    static constexpr int BOX_BYTES = BOX * (int)sizeof(T);
+    static constexpr int BOX_PAD = (BOX_BYTES + 127) / 128 * 128 / (int)sizeof(T);  // 128 B aligned slots
+    static constexpr int WX = TX / 32, WY = (NT / 32) / WX, CY = TY / WY;
+    static constexpr int RING = 2 * TX + 2 * TY;
+    static_assert(TX % 32 == 0 && (NT / 32) % WX == 0 && TY % WY == 0, "tile/warp mismatch");
+    static_assert(RING <= NT, "one ring position per thread");
+    static_assert(BX * sizeof(T) % 16 == 0 && (XH * sizeof(T)) % 16 == 0, "TMA box alignment");
+};
+
+template <typename T>
+struct alignas(128) TmaSmem {
+    using G = TmaGeo<T>;
+    T raw[G::S][3][G::BOX_PAD];   // etaS, etaL, c boxes per stage
+    T mm[3][2][G::BOX];           // mu, M of three consecutive planes
+    unsigned long long bar[G::S];
+    int abort;
+};
+
+template <typename T>
+size_t tma_smem_bytes() { return sizeof(TmaSmem<T>) + 128; }
+
+// ------------------------------------------------------------ PTX glue ----
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait on an mbarrier phase; false when the time limit ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer();
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try(bar, parity)) return true;
+        if ((it & 31u) == 31u && globaltimer() - t0 > limit_ns) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(dst),
+        "l"((unsigned long long)map), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+template <typename T>
+__device__ __forceinline__ T fast_rcp(T x);
+template <>
+__device__ __forceinline__ float fast_rcp<float>(float x) { return __fdividef(1.0f, x); }
+template <>
+__device__ __forceinline__ double fast_rcp<double>(double x) { return __drcp_rn(x); }
+
+// pass A (phasefield.c:328-332) for a neighbour-only cell: mu and M
+template <typename T>
+__device__ __forceinline__ void pass_a(const Coef<T> &k, T eS, T eL, T c, T &mu, T &M) {
+    const T rs = fast_rcp(eS * eS + eL * eL);
+    const T h = eS * eS * rs;
+    const T rA = fast_rcp(k.AS + k.dA * h);
+    mu = k.AsAl * rA * (c - k.cL0 + k.dc0 * h);
+    M = k.ML + k.dM * h;
+}
+
+// pass A for an owned cell, plus the centre-only part of pass B: the KKS
+// phase compositions, the parabolas and the driving force dmu
+// (phasefield.c:351-359), so that only (etaS, etaL, c, mu, M, dmu) travel
+// from one plane to the next
+template <typename T>
+__device__ __forceinline__ void pass_a_own(const Coef<T> &k, T eS, T eL, T c, T &mu, T &M, T &dmu) {
+    const T rs = fast_rcp(eS * eS + eL * eL);
+    const T h = eS * eS * rs;
+    const T rA = fast_rcp(k.AS + k.dA * h);
+    mu = k.AsAl * rA * (c - k.cL0 + k.dc0 * h);
+    M = k.ML + k.dM * h;
+    const T cSp = rA * (k.AL * c + (T(1) - h) * k.tmp2);
+    const T cLp = rA * (k.AS * c - h * k.tmp2);
+    const T fS = k.halfAS * (cSp - k.cS0) * (cSp - k.cS0) + k.CS;
+    const T fL = k.halfAL * (cLp - k.cL0) * (cLp - k.cL0) + k.CL;
+    dmu = T(2) * (eS * eL) * (rs * rs) * (fS - fL - mu * (cSp - cLp));
+}
+
+__device__ __forceinline__ void ghosts_of(int i, int n, int bc, int &g0, int &g1) {
+    g0 = -2;
+    g1 = -2;
+    if (i == 0) g0 = (bc == 0) ? n : -1;
+    if (i == n - 1) g1 = (bc == 0) ? -1 : n;
+}
+
+template <typename T, bool C_ONLY>
+__device__ __forceinline__ void put(const Geom &g, const Fields<T> &o, int64_t i, T s, T l, T c) {
+    if (!C_ONLY) {
+        o.eS[i] = s;
+        o.eL[i] = l;
+    }
+    o.c[i] = c;
+}
+
+// the new state of cell (x,y,z) and every face ghost that mirrors it
+template <typename T, bool C_ONLY>
+__device__ __forceinline__ void store_cell(const Geom &g, const Fields<T> &o, int x, int y, int z, T s, T l, T c) {
+    put<T, C_ONLY>(g, o, g.at(x, y, z), s, l, c);
+    if (x == 0 || y == 0 || z == 0 || x == g.nx - 1 || y == g.ny - 1 || z == g.nz - 1) {
+        int a, b;
+        ghosts_of(x, g.nx, g.bc, a, b);
+        if (a != -2) put<T, C_ONLY>(g, o, g.at(a, y, z), s, l, c);
+        if (b != -2) put<T, C_ONLY>(g, o, g.at(b, y, z), s, l, c);
+        ghosts_of(y, g.ny, g.bc, a, b);
+        if (a != -2) put<T, C_ONLY>(g, o, g.at(x, a, z), s, l, c);
+        if (b != -2) put<T, C_ONLY>(g, o, g.at(x, b, z), s, l, c);
+        ghosts_of(z, g.nz, g.bc, a, b);
+        if (a != -2) put<T, C_ONLY>(g, o, g.at(x, y, a), s, l, c);
+        if (b != -2) put<T, C_ONLY>(g, o, g.at(x, y, b), s, l, c);
+    }
+}
+
+// Walks the load sequence of one CTA: for every tile-column segment of its
+// flat (tile, z) range, the planes z0-1 .. z1 (z1 exclusive end + its halo).
+struct SegWalk {
+    int64_t s, s1;     // flat range still to visit
+    int nz, tile, z0, z1, pz;
+    __device__ void start(int64_t a, int64_t b, int nz_) {
+        s = a; s1 = b; nz = nz_;
+        seg();
+    }
+    __device__ void seg() {
+        if (s >= s1) { tile = -1; return; }
+        tile = (int)(s / nz);
+        z0 = (int)(s % nz);
+        const int64_t left = s1 - s;
+        z1 = (int)((int64_t)z0 + left < (int64_t)nz ? (int64_t)z0 + left : (int64_t)nz);
+        pz = z0 - 1;
+    }
+    __device__ bool valid() const { return tile >= 0; }
+    __device__ void next_segment() {
+        s += (z1 - z0);
+        seg();
+    }
+    __device__ void advance() {       // to the next load
+        if (++pz > z1) next_segment();
+    }
+};
+
+template <typename T, bool STATS, bool C_ONLY>
+__global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
+    step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
+                    const __grid_constant__ CUtensorMap mapC, Geom g, Coef<T> k, Fields<T> out, int ntx, int nty,
+                    double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
+                    int inject_stall) {
+    using G = TmaGeo<T>;
+    constexpr int TX = G::TX, TY = G::TY, S = G::S, XH = G::XH, BX = G::BX, CY = G::CY;
+    extern __shared__ unsigned char smem_dyn[];
+    TmaSmem<T> &sm = *reinterpret_cast<TmaSmem<T> *>((reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~uintptr_t(127));
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = (warp % G::WX) * 32 + lane;        // own column in the tile
+    const int ty0 = (warp / G::WX) * CY;              // first own row in the tile
+    const int64_t total = (int64_t)ntx * nty * g.nz;
+    const int64_t per = (total + gridDim.x - 1) / gridDim.x;
+    const int64_t s0 = (int64_t)blockIdx.x * per;
+    const int64_t s1 = s0 + per < total ? s0 + per : total;
+
+    double acc[3] = {0.0, 0.0, 0.0};
+    if (s0 < s1) {
+        if (tid == 0) {
+            for (int s = 0; s < S; ++s) mbar_init(smem_u32(&sm.bar[s]), 1);
+            sm.abort = 0;
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        __syncthreads();
+
+        // producer state (thread 0): the next load to issue
+        SegWalk prod;
+        int64_t issued = 0;
+        auto issue = [&](int64_t l) {
+            const int st = (int)(l % S);
+            const uint32_t bar = smem_u32(&sm.bar[st]);
+            const int bx = prod.tile % ntx, by = prod.tile / ntx;
+            const int xs = bx * TX + g.xoff - XH;     // storage x of the box start (16-byte aligned)
+            const int ys = by * TY;                    // storage y of interior y0-1
+            const int zs = prod.pz + 1;                // storage z of the plane
+            uint32_t bytes = 3u * (uint32_t)G::BOX_BYTES;
+            if (inject_stall && l == 1) bytes += 16u;  // test hook: this phase can never complete
+            mbar_expect_tx(bar, bytes);
+            tma_load_3d(smem_u32(sm.raw[st][0]), &mapS, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[st][1]), &mapL, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[st][2]), &mapC, xs, ys, zs, bar);
+            prod.advance();
+        };
+        prod.start(s0, s1, g.nz);
+        if (tid == 0)
+            for (int l = 0; l < S - 2 && prod.valid(); ++l) issue(issued++);
+
+        // registers of the own cells: plane q-1 (p*), plane q (q*), plane q+1 (x*)
+        T pS[CY], pL[CY], pmu[CY], pM[CY];
+        T qS[CY], qL[CY], qmu[CY], qM[CY], qc[CY], qd[CY];
+        T xS[CY], xL[CY], xmu[CY], xM[CY], xc[CY], xd[CY];
+#pragma unroll
+        for (int j = 0; j < CY; ++j) {
+            pS[j] = pL[j] = pmu[j] = pM[j] = T(0);
+            qS[j] = qL[j] = qmu[j] = qM[j] = qc[j] = qd[j] = T(0);
+        }
+
+        SegWalk cons;
+        cons.start(s0, s1, g.nz);
+        int64_t l = 0;                                  // load index being consumed
+        bool dead = false;
+        while (cons.valid() && !dead) {
+            const int bx = cons.tile % ntx, by = cons.tile / ntx;
+            const int x0 = bx * TX, y0 = by * TY, z0 = cons.z0, z1 = cons.z1;
+            const int X = x0 + tx;
+            for (int pz = z0 - 1; pz <= z1; ++pz, ++l) {
+                const int st = (int)(l % S);
+                const uint32_t par = (uint32_t)((l / S) & 1);
+                if (!mbar_wait(smem_u32(&sm.bar[st]), par, limit_ns)) {
+                    sm.abort = 1;
+                    atomicOr(err, 1);
+                }
+                const T *rS = sm.raw[st][0], *rL = sm.raw[st][1], *rC = sm.raw[st][2];
+                T *wmu = sm.mm[l % 3][0], *wM = sm.mm[l % 3][1];
+                // pass A: own cells into registers and shared memory
+#pragma unroll
+                for (int j = 0; j < CY; ++j) {
+                    const int o = (ty0 + j + 1) * BX + tx + XH;
+                    xS[j] = rS[o];
+                    xL[j] = rL[o];
+                    xc[j] = rC[o];
+                    if (C_ONLY) {
+                        pass_a(k, xS[j], xL[j], xc[j], xmu[j], xM[j]);
+                        xd[j] = T(0);
+                    } else {
+                        pass_a_own(k, xS[j], xL[j], xc[j], xmu[j], xM[j], xd[j]);
+                    }
+                    wmu[o] = xmu[j];
+                    wM[o] = xM[j];
+                }
+                // pass A: the one-cell ring around the tile
+                if (tid < G::RING) {
+                    int hx, hy;
+                    if (tid < TX) { hx = tid; hy = -1; }
+                    else if (tid < 2 * TX) { hx = tid - TX; hy = TY; }
+                    else if (tid < 2 * TX + TY) { hx = -1; hy = tid - 2 * TX; }
+                    else { hx = TX; hy = tid - 2 * TX - TY; }
+                    const int o = (hy + 1) * BX + hx + XH;
+                    T mu, M;
+                    pass_a(k, rS[o], rL[o], rC[o], mu, M);
+                    wmu[o] = mu;
+                    wM[o] = M;
+                }
+                __syncthreads();
+                if (sm.abort) { dead = true; break; }
+                if (tid == 0 && prod.valid()) issue(issued++);   // refill the stage freed two planes ago
+
+                // pass B + C for plane q = pz - 1
+                const int q = pz - 1;
+                if (q >= z0) {
+                    const int sq = (int)((l - 1) % S);
+                    const T *nS = sm.raw[sq][0], *nL = sm.raw[sq][1];
+                    const T *nmu = sm.mm[(l - 1) % 3][0], *nM = sm.mm[(l - 1) % 3][1];
+#pragma unroll
+                    for (int j = 0; j < CY; ++j) {
+                        const int Y = y0 + ty0 + j;
+                        if (X < g.nx && Y < g.ny) {
+                            const int o = (ty0 + j + 1) * BX + tx + XH;
+                            const T mu = qmu[j], M = qM[j];
+                            const T muym = j > 0 ? qmu[j - 1] : nmu[o - BX], Mym = j > 0 ? qM[j - 1] : nM[o - BX];
+                            const T muyp = j < CY - 1 ? qmu[j + 1] : nmu[o + BX];
+                            const T Myp = j < CY - 1 ? qM[j + 1] : nM[o + BX];
+                            // solute: flux form of phasefield.c:374-384
+                            const T fl = (xM[j] + M) * (xmu[j] - mu) + (pM[j] + M) * (pmu[j] - mu) +
+                                         (Myp + M) * (muyp - mu) + (Mym + M) * (muym - mu) +
+                                         (nM[o + 1] + M) * (nmu[o + 1] - mu) + (nM[o - 1] + M) * (nmu[o - 1] - mu);
+                            const T dc = k.tmp3 * fl;
+                            const T c = qc[j];
+                            if (C_ONLY) {
+                                store_cell<T, true>(g, out, X, Y, q, T(0), T(0), c + dc);
+                                if (STATS) acc[0] += (double)dc * (double)dc;
+                            } else {
+                                const T eS = qS[j], eL = qL[j], dmu = qd[j];
+                                const T Sym = j > 0 ? qS[j - 1] : nS[o - BX], Syp = j < CY - 1 ? qS[j + 1] : nS[o + BX];
+                                const T Lym = j > 0 ? qL[j - 1] : nL[o - BX], Lyp = j < CY - 1 ? qL[j + 1] : nL[o + BX];
+                                // detaS, detaL: phasefield.c:360-373
+                                const T lapS = xS[j] + pS[j] + Syp + Sym + nS[o + 1] + nS[o - 1] - T(6) * eS;
+                                const T lapL = xL[j] + pL[j] + Lyp + Lym + nL[o + 1] + nL[o - 1] - T(6) * eL;
+                                const T dS = k.tmp1 * (k.m * eS * (eS * eS - T(1) + k.twogam * eL * eL) - k.kh2 * lapS + eL * dmu);
+                                const T dL = k.tmp1 * (k.m * eL * (eL * eL - T(1) + k.twogam * eS * eS) - k.kh2 * lapL - eS * dmu);
+                                store_cell<T, false>(g, out, X, Y, q, eS + dS, eL + dL, c + dc);
+                                if (STATS) {
+                                    acc[0] += (double)dc * (double)dc;
+                                    acc[1] += (double)dS * (double)dS;
+                                    acc[2] += (double)dL * (double)dL;
+                                }
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < CY; ++j) {
+                    pS[j] = qS[j]; pL[j] = qL[j]; pmu[j] = qmu[j]; pM[j] = qM[j];
+                    qS[j] = xS[j]; qL[j] = xL[j]; qmu[j] = xmu[j]; qM[j] = xM[j];
+                    qc[j] = xc[j]; qd[j] = xd[j];
+                }
+            }
+            if (!dead) cons.next_segment();
+        }
+        if (dead) {
+            // drain this CTA's own copies still in flight (bounded), then leave
+            if (tid == 0)
+                for (int64_t d = l; d < issued; ++d)
+                    (void)mbar_wait(smem_u32(&sm.bar[d % S]), (uint32_t)((d / S) & 1), limit_ns);
+            return;
+        }
+    }
+    if (STATS) {
+        // block sum -> partials[blockIdx.x * 3 + i]
+        __shared__ double red[TmaGeo<T>::NT / 32][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            double v = acc[i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[warp][i] = v;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int i = 0; i < 3; ++i) {
+                double s = 0;
+                for (int w = 0; w < TmaGeo<T>::NT / 32; ++w) s += red[w][i];
+                partials[(int64_t)blockIdx.x * 3 + i] = s;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host --
+
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+template <typename T>
+int make_field_map(const Geom &g, const T *base, CUtensorMap *map) {
+    using G = TmaGeo<T>;
+    auto enc = get_encode();
+    if (!enc) return -1;
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || ((g.P * sizeof(T)) & 15)) return -2;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.P, (cuuint64_t)(g.ny + 2), (cuuint64_t)(g.nz + 2)};
+    const cuuint64_t strides[2] = {(cuuint64_t)(g.P * sizeof(T)), (cuuint64_t)(g.PS * sizeof(T))};
+    const cuuint32_t box[3] = {(cuuint32_t)G::BX, (cuuint32_t)G::BY, 1u};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    CUresult r = enc(map, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                     (void *)base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? 0 : -3;
+}
+
+template <typename T>
+static cudaError_t set_attrs() {
+    const int bytes = (int)tma_smem_bytes<T>();
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    return cudaFuncSetAttribute(step_tma_kernel<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <typename T>
+int tma_grid(const Geom &g, int num_sms) {
+    using G = TmaGeo<T>;
+    // kernel attributes are per device: set them once for each
+    static int occ_of[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+    int &occ = occ_of[dev];
+    if (!occ) {
+        if (set_attrs<T>() != cudaSuccess) return -1;
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false>, G::NT,
+                                                          tma_smem_bytes<T>()) != cudaSuccess || o < 1)
+            o = 1;
+        occ = o;
+    }
+    const int64_t ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
+    const int64_t total = ntx * nty * g.nz;
+    int64_t grid = (int64_t)occ * num_sms;
+    if (grid > total) grid = total;
+    return (int)grid;
+}
+
+template <typename T>
+cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
+                            double *partials, int grid, int *err, unsigned long long limit_ns, int inject_stall,
+                            cudaStream_t s) {
+    using G = TmaGeo<T>;
+    const int ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
+    const size_t sh = tma_smem_bytes<T>();
+    const bool st = partials != nullptr;
+#define PPF_LAUNCH(ST, CO)                                                                                       \
+    step_tma_kernel<T, ST, CO><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty, partials, \
+                                                       err, limit_ns, inject_stall)
+    if (!c_only) {
+        if (st) PPF_LAUNCH(true, false);
+        else PPF_LAUNCH(false, false);
+    } else {
+        if (st) PPF_LAUNCH(true, true);
+        else PPF_LAUNCH(false, true);
+    }
+#undef PPF_LAUNCH
+    return cudaGetLastError();
+}
+
+template int make_field_map<float>(const Geom &, const float *, CUtensorMap *);
+template int make_field_map<double>(const Geom &, const double *, CUtensorMap *);
+template int tma_grid<float>(const Geom &, int);
+template int tma_grid<double>(const Geom &, int);
+template cudaError_t launch_step_tma<float>(const Geom &, const Coef<float> &, const CUtensorMap *, Fields<float>,
+                                            bool, double *, int, int *, unsigned long long, int, cudaStream_t);
+template cudaError_t launch_step_tma<double>(const Geom &, const Coef<double> &, const CUtensorMap *,
+                                             Fields<double>, bool, double *, int, int *, unsigned long long, int,
+                                             cudaStream_t);
+
+}  // namespace ppf

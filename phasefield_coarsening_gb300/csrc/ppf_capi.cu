@@ -55,6 +55,7 @@ struct ppf_ctx {
     int *derr;            // device error word set by a kernel whose bounded wait ran out
     CUtensorMap maps[2][3];   // TMA maps of the fields of both buffers
     int grid;             // persistent grid of the fused step
+    int zc;               // z chunk of one work item
     unsigned long long wait_limit_ns;
     int inject;           // test hook: PPF_INJECT_*
     int64_t steps;
@@ -210,7 +211,8 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
                 return seterr(PPF_ECUDA, "TMA descriptor setup failed (%d)", mr);
             }
         }
-    c->grid = precision == PPF_F32 ? tma_grid<float>(c->g, c->num_sms) : tma_grid<double>(c->g, c->num_sms);
+    c->grid = precision == PPF_F32 ? tma_grid<float>(c->g, c->num_sms, &c->zc)
+                                   : tma_grid<double>(c->g, c->num_sms, &c->zc);
     if (c->grid < 1) {
         ppf_destroy(c);
         return seterr(PPF_ECUDA, "kernel attribute setup failed");
@@ -354,12 +356,12 @@ static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
         cudaError_t e;
         if (c->prec == PPF_F32) {
             const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
-            e = launch_step_tma<float>(c->g, c->kf, m, ff(c, oe, oc), c_only, part, c->grid, c->derr,
-                                       c->wait_limit_ns, inject, c->stream);
+            e = launch_step_tma<float>(c->g, c->kf, m, ff(c, oe, oc), c_only, part, c->grid, c->zc,
+                                       c->derr, c->wait_limit_ns, inject, c->stream);
         } else {
             const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
-            e = launch_step_tma<double>(c->g, c->kd, m, fd(c, oe, oc), c_only, part, c->grid, c->derr,
-                                        c->wait_limit_ns, inject, c->stream);
+            e = launch_step_tma<double>(c->g, c->kd, m, fd(c, oe, oc), c_only, part, c->grid, c->zc,
+                                        c->derr, c->wait_limit_ns, inject, c->stream);
         }
         if (e != cudaSuccess) return seterr(PPF_ECUDA, "step launch failed: %s", cudaGetErrorString(e));
         c->cur_eta = oe;

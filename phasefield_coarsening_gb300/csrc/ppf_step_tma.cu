@@ -6,8 +6,8 @@
 // :393-401 pass C) -- or of sweep_fields_c (:406-476) in c-only mode.
 //
 // Data flow of one CTA:
-//   * a contiguous range of (x-y tile, z plane) work, balanced over the
-//     persistent grid; each tile column segment is marched up z;
+//   * (z chunk, x-y tile) work items in chunk-major order, dealt round-robin
+//     to a persistent grid; each item is a tile column segment marched up z;
 //   * thread 0 streams every plane's etaS/etaL/c tile plus a one-cell ring
 //     (a TX+2*XH by TY+2 box per field) from HBM into a S-stage shared ring
 //     with cp.async.bulk.tensor.3d, completion signalled on an mbarrier per
@@ -188,38 +188,36 @@ __device__ __forceinline__ void store_cell(const Geom &g, const Fields<T> &o, in
     }
 }
 
-// Walks the load sequence of one CTA: for every tile-column segment of its
-// flat (tile, z) range, the planes z0-1 .. z1 (z1 exclusive end + its halo).
-struct SegWalk {
-    int64_t s, s1;     // flat range still to visit
-    int nz, tile, z0, z1, pz;
-    __device__ void start(int64_t a, int64_t b, int nz_) {
-        s = a; s1 = b; nz = nz_;
-        seg();
+// Work items are (z chunk, x-y tile) pairs in chunk-major order, dealt
+// round-robin to the persistent CTAs: CTAs resident at the same time march
+// the same z window of neighbouring tiles, so the halo rows one tile reads
+// from its neighbours' data are still in L2.  A walker yields the load
+// sequence of one CTA: for each of its items, planes z0-1 .. z1.
+struct ItemWalk {
+    int item, stride, nitems, ntiles, zc, nz;
+    int tile, z0, z1, pz;
+    __device__ __forceinline__ void start(int first, int stride_, int nitems_, int ntiles_, int zc_, int nz_) {
+        item = first; stride = stride_; nitems = nitems_; ntiles = ntiles_; zc = zc_; nz = nz_;
+        set();
     }
-    __device__ void seg() {
-        if (s >= s1) { tile = -1; return; }
-        tile = (int)(s / nz);
-        z0 = (int)(s % nz);
-        const int64_t left = s1 - s;
-        z1 = (int)((int64_t)z0 + left < (int64_t)nz ? (int64_t)z0 + left : (int64_t)nz);
+    __device__ __forceinline__ void set() {
+        if (item >= nitems) { tile = -1; return; }
+        const int c = item / ntiles;
+        tile = item - c * ntiles;
+        z0 = c * zc;
+        z1 = min(nz, z0 + zc);
         pz = z0 - 1;
     }
-    __device__ bool valid() const { return tile >= 0; }
-    __device__ void next_segment() {
-        s += (z1 - z0);
-        seg();
-    }
-    __device__ void advance() {       // to the next load
-        if (++pz > z1) next_segment();
-    }
+    __device__ __forceinline__ bool valid() const { return tile >= 0; }
+    __device__ __forceinline__ void next_item() { item += stride; set(); }
+    __device__ __forceinline__ void advance() { if (++pz > z1) next_item(); }
 };
 
 template <typename T, bool STATS, bool C_ONLY>
 __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
                     const __grid_constant__ CUtensorMap mapC, Geom g, Coef<T> k, Fields<T> out, int ntx, int nty,
-                    double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
+                    int zc, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
                     int inject_stall) {
     using G = TmaGeo<T>;
     constexpr int TX = G::TX, TY = G::TY, S = G::S, XH = G::XH, BX = G::BX, CY = G::CY;
@@ -229,13 +227,12 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = (warp % G::WX) * 32 + lane;        // own column in the tile
     const int ty0 = (warp / G::WX) * CY;              // first own row in the tile
-    const int64_t total = (int64_t)ntx * nty * g.nz;
-    const int64_t per = (total + gridDim.x - 1) / gridDim.x;
-    const int64_t s0 = (int64_t)blockIdx.x * per;
-    const int64_t s1 = s0 + per < total ? s0 + per : total;
+    const int ntiles = ntx * nty;
+    const int nitems = ntiles * ((g.nz + zc - 1) / zc);
+    const int ob = (ty0 + 1) * BX + tx + XH;          // shared offset of the first own cell
 
     double acc[3] = {0.0, 0.0, 0.0};
-    if (s0 < s1) {
+    if ((int)blockIdx.x < nitems) {
         if (tid == 0) {
             for (int s = 0; s < S; ++s) mbar_init(smem_u32(&sm.bar[s]), 1);
             sm.abort = 0;
@@ -244,27 +241,28 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
         }
         __syncthreads();
 
-        // producer state (thread 0): the next load to issue
-        SegWalk prod;
-        int64_t issued = 0;
-        auto issue = [&](int64_t l) {
-            const int st = (int)(l % S);
-            const uint32_t bar = smem_u32(&sm.bar[st]);
+        // producer (thread 0): next load to issue, its stage, loads issued
+        ItemWalk prod;
+        prod.start(blockIdx.x, gridDim.x, nitems, ntiles, zc, g.nz);
+        int ist = 0, issued = 0;
+        auto issue = [&]() {
+            const uint32_t bar = smem_u32(&sm.bar[ist]);
             const int bx = prod.tile % ntx, by = prod.tile / ntx;
             const int xs = bx * TX + g.xoff - XH;     // storage x of the box start (16-byte aligned)
             const int ys = by * TY;                    // storage y of interior y0-1
             const int zs = prod.pz + 1;                // storage z of the plane
             uint32_t bytes = 3u * (uint32_t)G::BOX_BYTES;
-            if (inject_stall && l == 1) bytes += 16u;  // test hook: this phase can never complete
+            if (inject_stall && issued == 1) bytes += 16u;   // test hook: this phase can never complete
             mbar_expect_tx(bar, bytes);
-            tma_load_3d(smem_u32(sm.raw[st][0]), &mapS, xs, ys, zs, bar);
-            tma_load_3d(smem_u32(sm.raw[st][1]), &mapL, xs, ys, zs, bar);
-            tma_load_3d(smem_u32(sm.raw[st][2]), &mapC, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][0]), &mapS, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][1]), &mapL, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][2]), &mapC, xs, ys, zs, bar);
             prod.advance();
+            ist = ist + 1 == S ? 0 : ist + 1;
+            ++issued;
         };
-        prod.start(s0, s1, g.nz);
         if (tid == 0)
-            for (int l = 0; l < S - 2 && prod.valid(); ++l) issue(issued++);
+            for (int l = 0; l < S - 2 && prod.valid(); ++l) issue();
 
         // registers of the own cells: plane q-1 (p*), plane q (q*), plane q+1 (x*)
         T pS[CY], pL[CY], pmu[CY], pM[CY];
@@ -276,27 +274,30 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             qS[j] = qL[j] = qmu[j] = qM[j] = qc[j] = qd[j] = T(0);
         }
 
-        SegWalk cons;
-        cons.start(s0, s1, g.nz);
-        int64_t l = 0;                                  // load index being consumed
+        ItemWalk cons;
+        cons.start(blockIdx.x, gridDim.x, nitems, ntiles, zc, g.nz);
+        int st = 0, mb = 0, consumed = 0;            // stage / mu-M buffer / count of the current load
+        uint32_t par = 0;
+        int st_prev = 0, mb_prev = 0;
         bool dead = false;
         while (cons.valid() && !dead) {
             const int bx = cons.tile % ntx, by = cons.tile / ntx;
             const int x0 = bx * TX, y0 = by * TY, z0 = cons.z0, z1 = cons.z1;
             const int X = x0 + tx;
-            for (int pz = z0 - 1; pz <= z1; ++pz, ++l) {
-                const int st = (int)(l % S);
-                const uint32_t par = (uint32_t)((l / S) & 1);
+            // no own cell of this item touches a domain face in x or y, and all are inside
+            const bool inner_xy = x0 > 0 && x0 + TX < g.nx && y0 > 0 && y0 + TY < g.ny;
+            const int64_t col = (int64_t)(y0 + ty0 + 1) * g.P + X + g.xoff;   // storage of own cell j=0, z=-1
+            for (int pz = z0 - 1; pz <= z1; ++pz) {
                 if (!mbar_wait(smem_u32(&sm.bar[st]), par, limit_ns)) {
                     sm.abort = 1;
                     atomicOr(err, 1);
                 }
                 const T *rS = sm.raw[st][0], *rL = sm.raw[st][1], *rC = sm.raw[st][2];
-                T *wmu = sm.mm[l % 3][0], *wM = sm.mm[l % 3][1];
+                T *wmu = sm.mm[mb][0], *wM = sm.mm[mb][1];
                 // pass A: own cells into registers and shared memory
 #pragma unroll
                 for (int j = 0; j < CY; ++j) {
-                    const int o = (ty0 + j + 1) * BX + tx + XH;
+                    const int o = ob + j * BX;
                     xS[j] = rS[o];
                     xL[j] = rL[o];
                     xc[j] = rC[o];
@@ -324,19 +325,20 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 }
                 __syncthreads();
                 if (sm.abort) { dead = true; break; }
-                if (tid == 0 && prod.valid()) issue(issued++);   // refill the stage freed two planes ago
+                if (tid == 0 && prod.valid()) issue();   // refill the stage freed two planes ago
 
                 // pass B + C for plane q = pz - 1
                 const int q = pz - 1;
                 if (q >= z0) {
-                    const int sq = (int)((l - 1) % S);
-                    const T *nS = sm.raw[sq][0], *nL = sm.raw[sq][1];
-                    const T *nmu = sm.mm[(l - 1) % 3][0], *nM = sm.mm[(l - 1) % 3][1];
+                    const T *nS = sm.raw[st_prev][0], *nL = sm.raw[st_prev][1];
+                    const T *nmu = sm.mm[mb_prev][0], *nM = sm.mm[mb_prev][1];
+                    const bool inner = inner_xy && q > 0 && q < g.nz - 1;
+                    const int64_t base = col + (int64_t)(q + 1) * g.PS;
 #pragma unroll
                     for (int j = 0; j < CY; ++j) {
                         const int Y = y0 + ty0 + j;
-                        if (X < g.nx && Y < g.ny) {
-                            const int o = (ty0 + j + 1) * BX + tx + XH;
+                        if (inner || (X < g.nx && Y < g.ny)) {
+                            const int o = ob + j * BX;
                             const T mu = qmu[j], M = qM[j];
                             const T muym = j > 0 ? qmu[j - 1] : nmu[o - BX], Mym = j > 0 ? qM[j - 1] : nM[o - BX];
                             const T muyp = j < CY - 1 ? qmu[j + 1] : nmu[o + BX];
@@ -347,8 +349,10 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                                          (nM[o + 1] + M) * (nmu[o + 1] - mu) + (nM[o - 1] + M) * (nmu[o - 1] - mu);
                             const T dc = k.tmp3 * fl;
                             const T c = qc[j];
+                            const int64_t a = base + (int64_t)j * g.P;
                             if (C_ONLY) {
-                                store_cell<T, true>(g, out, X, Y, q, T(0), T(0), c + dc);
+                                if (inner) out.c[a] = c + dc;
+                                else store_cell<T, true>(g, out, X, Y, q, T(0), T(0), c + dc);
                                 if (STATS) acc[0] += (double)dc * (double)dc;
                             } else {
                                 const T eS = qS[j], eL = qL[j], dmu = qd[j];
@@ -359,7 +363,13 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                                 const T lapL = xL[j] + pL[j] + Lyp + Lym + nL[o + 1] + nL[o - 1] - T(6) * eL;
                                 const T dS = k.tmp1 * (k.m * eS * (eS * eS - T(1) + k.twogam * eL * eL) - k.kh2 * lapS + eL * dmu);
                                 const T dL = k.tmp1 * (k.m * eL * (eL * eL - T(1) + k.twogam * eS * eS) - k.kh2 * lapL - eS * dmu);
-                                store_cell<T, false>(g, out, X, Y, q, eS + dS, eL + dL, c + dc);
+                                if (inner) {
+                                    out.eS[a] = eS + dS;
+                                    out.eL[a] = eL + dL;
+                                    out.c[a] = c + dc;
+                                } else {
+                                    store_cell<T, false>(g, out, X, Y, q, eS + dS, eL + dL, c + dc);
+                                }
                                 if (STATS) {
                                     acc[0] += (double)dc * (double)dc;
                                     acc[1] += (double)dS * (double)dS;
@@ -375,14 +385,19 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     qS[j] = xS[j]; qL[j] = xL[j]; qmu[j] = xmu[j]; qM[j] = xM[j];
                     qc[j] = xc[j]; qd[j] = xd[j];
                 }
+                st_prev = st;
+                mb_prev = mb;
+                if (++st == S) { st = 0; par ^= 1u; }
+                mb = mb + 1 == 3 ? 0 : mb + 1;
+                ++consumed;
             }
-            if (!dead) cons.next_segment();
+            if (!dead) cons.next_item();
         }
         if (dead) {
             // drain this CTA's own copies still in flight (bounded), then leave
             if (tid == 0)
-                for (int64_t d = l; d < issued; ++d)
-                    (void)mbar_wait(smem_u32(&sm.bar[d % S]), (uint32_t)((d / S) & 1), limit_ns);
+                for (int d = 0; d < issued - consumed; ++d)
+                    (void)mbar_wait(smem_u32(&sm.bar[(st + d) % S]), par ^ (uint32_t)(((st + d) / S) & 1), limit_ns);
             return;
         }
     }
@@ -434,7 +449,7 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map) {
     const cuuint32_t estr[3] = {1u, 1u, 1u};
     CUresult r = enc(map, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
                      (void *)base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? 0 : -3;
 }
 
@@ -451,8 +466,10 @@ static cudaError_t set_attrs() {
     return cudaFuncSetAttribute(step_tma_kernel<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
+// Launch shape: z chunks of zc planes so that one wave of resident CTAs
+// covers all tiles of consecutive chunks; *zc_out receives the chunk.
 template <typename T>
-int tma_grid(const Geom &g, int num_sms) {
+int tma_grid(const Geom &g, int num_sms, int *zc_out) {
     using G = TmaGeo<T>;
     // kernel attributes are per device: set them once for each
     static int occ_of[64];
@@ -467,24 +484,31 @@ int tma_grid(const Geom &g, int num_sms) {
             o = 1;
         occ = o;
     }
-    const int64_t ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
-    const int64_t total = ntx * nty * g.nz;
-    int64_t grid = (int64_t)occ * num_sms;
-    if (grid > total) grid = total;
-    return (int)grid;
+    const int64_t ntiles = (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY);
+    const int64_t slots = (int64_t)occ * num_sms;
+    // as many chunks as fit one wave, but chunks of at least 8 planes
+    int64_t nc = slots / ntiles;
+    if (nc > g.nz / 8) nc = g.nz / 8;
+    if (nc < 1) nc = 1;
+    const int zc = (int)((g.nz + nc - 1) / nc);
+    nc = (g.nz + zc - 1) / zc;
+    const int64_t items = ntiles * nc;
+    if (items > (int64_t)1 << 30) return -1;
+    *zc_out = zc;
+    return (int)(items < slots ? items : slots);
 }
 
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
-                            double *partials, int grid, int *err, unsigned long long limit_ns, int inject_stall,
+                            double *partials, int grid, int zc, int *err, unsigned long long limit_ns, int inject_stall,
                             cudaStream_t s) {
     using G = TmaGeo<T>;
     const int ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
     const size_t sh = tma_smem_bytes<T>();
     const bool st = partials != nullptr;
 #define PPF_LAUNCH(ST, CO)                                                                                       \
-    step_tma_kernel<T, ST, CO><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty, partials, \
-                                                       err, limit_ns, inject_stall)
+    step_tma_kernel<T, ST, CO><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty, zc, \
+                                                       partials, err, limit_ns, inject_stall)
     if (!c_only) {
         if (st) PPF_LAUNCH(true, false);
         else PPF_LAUNCH(false, false);
@@ -498,12 +522,12 @@ cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *
 
 template int make_field_map<float>(const Geom &, const float *, CUtensorMap *);
 template int make_field_map<double>(const Geom &, const double *, CUtensorMap *);
-template int tma_grid<float>(const Geom &, int);
-template int tma_grid<double>(const Geom &, int);
+template int tma_grid<float>(const Geom &, int, int *);
+template int tma_grid<double>(const Geom &, int, int *);
 template cudaError_t launch_step_tma<float>(const Geom &, const Coef<float> &, const CUtensorMap *, Fields<float>,
-                                            bool, double *, int, int *, unsigned long long, int, cudaStream_t);
+                                            bool, double *, int, int, int *, unsigned long long, int, cudaStream_t);
 template cudaError_t launch_step_tma<double>(const Geom &, const Coef<double> &, const CUtensorMap *,
-                                             Fields<double>, bool, double *, int, int *, unsigned long long, int,
+                                             Fields<double>, bool, double *, int, int, int *, unsigned long long, int,
                                              cudaStream_t);
 
 }  // namespace ppf

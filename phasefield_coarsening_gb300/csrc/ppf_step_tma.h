@@ -13,9 +13,10 @@ namespace ppf {
 template <typename T>
 int make_field_map(const Geom &g, const T *base, CUtensorMap *map);
 
-// Persistent grid size (occupancy x SMs, capped by the work); < 0 on error.
+// Persistent grid size (occupancy x SMs, capped by the work) and the z
+// chunk length of a work item; < 0 on error.
 template <typename T>
-int tma_grid(const Geom &g, int num_sms);
+int tma_grid(const Geom &g, int num_sms, int *zc);
 
 // One fused step.  maps = {etaS, etaL, c} of the input state; `partials`
 // (nullable) receives 3 doubles per CTA; `err` is a device word that a
@@ -23,7 +24,7 @@ int tma_grid(const Geom &g, int num_sms);
 // test hook that makes one wait per CTA run out.
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
-                            double *partials, int grid, int *err, unsigned long long limit_ns, int inject_stall,
-                            cudaStream_t s);
+                            double *partials, int grid, int zc, int *err, unsigned long long limit_ns,
+                            int inject_stall, cudaStream_t s);
 
 }  // namespace ppf

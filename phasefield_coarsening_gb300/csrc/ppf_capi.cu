@@ -62,6 +62,7 @@ struct ppf_ctx {
     int uploaded;
     Coef<float> kf;
     Coef<double> kd;
+    int eqA;              // AS == AL: the mu reciprocal is a constant
     CoefD cd;
 };
 
@@ -106,26 +107,26 @@ extern "C" int ppf_params_derive(const ppf_params *p, ppf_derived *d) {
 
 template <typename T>
 static Coef<T> make_coef(const ppf_params &p, const ppf_derived &d) {
+    const double tmp1 = -1.0 * d.L * d.dt;         // :337
+    const double tmp3 = d.dt * 0.5 * d.h2;          // :339
+    const double kh2 = d.kappa * d.h2;
     Coef<T> k;
     k.AS = (T)p.AS;
-    k.AL = (T)p.AL;
     k.dA = (T)(p.AL - p.AS);
     k.AsAl = (T)(p.AS * p.AL);
-    k.cS0 = (T)p.cS0;
+    k.A = (T)p.AS;
     k.cL0 = (T)p.cL0;
     k.dc0 = (T)(p.cL0 - p.cS0);
-    k.CS = (T)p.CS;
-    k.CL = (T)p.CL;
-    k.halfAS = (T)(0.5 * p.AS);
-    k.halfAL = (T)(0.5 * p.AL);
-    k.ML = (T)d.ML;
-    k.dM = (T)(d.MS - d.ML);
-    k.tmp1 = (T)(-1.0 * d.L * d.dt);
-    k.tmp2 = (T)(p.AS * p.cS0 - p.AL * p.cL0);
-    k.tmp3 = (T)(d.dt * 0.5 * d.h2);
-    k.m = (T)d.m;
-    k.twogam = (T)(2.0 * p.gamma);
-    k.kh2 = (T)(d.kappa * d.h2);
+    k.Mt0 = (T)(tmp3 * d.ML);
+    k.Mt1 = (T)(tmp3 * (d.MS - d.ML));
+    k.dC = (T)(p.CS - p.CL);
+    k.q1 = (T)(p.cS0 - p.cL0);
+    k.q2 = (T)(0.5 * (1.0 / p.AS - 1.0 / p.AL));
+    k.dm2 = (T)(2.0 * tmp1);
+    k.mt = (T)(tmp1 * d.m);
+    k.g2 = (T)(2.0 * p.gamma * tmp1 * d.m);
+    k.e0 = (T)(6.0 * tmp1 * kh2 - tmp1 * d.m);
+    k.kt = (T)(tmp1 * kh2);
     return k;
 }
 
@@ -180,6 +181,7 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
     c->g = precision == PPF_F32 ? make_geom<float>(nz, ny, nx, bc) : make_geom<double>(nz, ny, nx, bc);
     c->kf = make_coef<float>(prm, der);
     c->kd = make_coef<double>(prm, der);
+    c->eqA = prm.AS == prm.AL;
     c->cd.AS = prm.AS; c->cd.AL = prm.AL; c->cd.dA = prm.AL - prm.AS;
     c->cd.cS0 = prm.cS0; c->cd.cL0 = prm.cL0; c->cd.CS = prm.CS; c->cd.CL = prm.CL;
     c->cd.tmp2 = prm.AS * prm.cS0 - prm.AL * prm.cL0;
@@ -356,12 +358,12 @@ static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
         cudaError_t e;
         if (c->prec == PPF_F32) {
             const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
-            e = launch_step_tma<float>(c->g, c->kf, m, ff(c, oe, oc), c_only, part, c->grid, c->zc,
-                                       c->derr, c->wait_limit_ns, inject, c->stream);
+            e = launch_step_tma<float>(c->g, c->kf, m, ff(c, oe, oc), c_only, c->eqA, part, c->grid,
+                                       c->zc, c->derr, c->wait_limit_ns, inject, c->stream);
         } else {
             const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
-            e = launch_step_tma<double>(c->g, c->kd, m, fd(c, oe, oc), c_only, part, c->grid, c->zc,
-                                        c->derr, c->wait_limit_ns, inject, c->stream);
+            e = launch_step_tma<double>(c->g, c->kd, m, fd(c, oe, oc), c_only, c->eqA, part, c->grid,
+                                        c->zc, c->derr, c->wait_limit_ns, inject, c->stream);
         }
         if (e != cudaSuccess) return seterr(PPF_ECUDA, "step launch failed: %s", cudaGetErrorString(e));
         c->cur_eta = oe;

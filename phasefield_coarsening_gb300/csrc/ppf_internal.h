@@ -36,17 +36,23 @@ Geom make_geom(int nz, int ny, int nx, int bc) {
     return g;
 }
 
-// Loop-invariant coefficients of sweep_fields (phasefield.c:322-323,
-// :337-339) and of the constants block (:76-97), folded on the host in
-// double and cast once to the step's precision.
+// Loop-invariant coefficients of the step, folded on the host in double
+// from the constants block (phasefield.c:76-97) and sweep_fields' own
+// invariants (tmp1..tmp6, :322-323, :337-339), then cast once to the
+// step's precision.  The folding rests on two exact identities of the KKS
+// construction of :351-359: with mu = AS AL/(AS+(AL-AS)hS) (c-cL0+(cL0-cS0)hS)
+// the phase compositions satisfy AS (cS-cS0) = AL (cL-cL0) = mu, hence
+//   fS - fL - mu (cS - cL) = (CS-CL) - mu ((cS0-cL0) + (1/AS-1/AL)/2 mu),
+// and detaS, detaL, dc of :360-384 are rearranged with tmp1, tmp3 absorbed.
 template <typename T>
 struct Coef {
-    T AS, AL, dA, AsAl;       // AS, AL, AL-AS, tmp5 = AS*AL
-    T cS0, cL0, dc0;          // cS0, cL0, tmp6 = cL0-cS0
-    T CS, CL, halfAS, halfAL; // parabola offsets, AS/2, AL/2
-    T ML, dM;                 // ML, MS-ML
-    T tmp1, tmp2, tmp3;       // -L*dt, AS*cS0-AL*cL0, dt*h2/2
-    T m, twogam, kh2;         // m, 2*gamma, kappa*h2
+    T AS, dA, AsAl;   // AS, AL-AS, AS*AL: mu = AsAl/(AS+dA h) (c-cL0+dc0 h)
+    T A;              // AS (= AL when eqA): mu = A (c-cL0+dc0 h)
+    T cL0, dc0;       // cL0, cL0-cS0
+    T Mt0, Mt1;       // tmp3*ML, tmp3*(MS-ML): M' = tmp3 M = Mt0 + Mt1 h
+    T dC, q1, q2;     // CS-CL, cS0-cL0, (1/AS-1/AL)/2: driving force D = dC - mu (q1 + q2 mu)
+    T dm2;            // 2 tmp1: tmp1 dmu = dm2 etaS etaL / (etaS^2+etaL^2)^2 D
+    T mt, g2, e0, kt; // tmp1 m, 2 gamma tmp1 m, 6 tmp1 kappa h2 - tmp1 m, tmp1 kappa h2
 };
 
 // The same coefficients in double, plus what the observables need.

@@ -126,32 +126,29 @@ __device__ __forceinline__ float fast_rcp<float>(float x) { return __fdividef(1.
 template <>
 __device__ __forceinline__ double fast_rcp<double>(double x) { return __drcp_rn(x); }
 
-// pass A (phasefield.c:328-332) for a neighbour-only cell: mu and M
-template <typename T>
-__device__ __forceinline__ void pass_a(const Coef<T> &k, T eS, T eL, T c, T &mu, T &M) {
-    const T rs = fast_rcp(eS * eS + eL * eL);
-    const T h = eS * eS * rs;
-    const T rA = fast_rcp(k.AS + k.dA * h);
-    mu = k.AsAl * rA * (c - k.cL0 + k.dc0 * h);
-    M = k.ML + k.dM * h;
+// pass A (phasefield.c:328-332) for one cell: mu and M' = tmp3 M.  With
+// EQ (AS == AL) the denominator AS+(AL-AS)hS is the constant AS and mu =
+// AS (c - cL0 + (cL0-cS0) hS).  Returns 1/(etaS^2+etaL^2) for reuse.
+template <typename T, bool EQ>
+__device__ __forceinline__ T pass_a(const Coef<T> &k, T eS, T eL, T c, T &mu, T &Mt) {
+    const T s2 = eS * eS;
+    const T rs = fast_rcp(s2 + eL * eL);
+    const T h = s2 * rs;
+    const T w = c - k.cL0 + k.dc0 * h;
+    if (EQ) mu = k.A * w;
+    else mu = k.AsAl * fast_rcp(k.AS + k.dA * h) * w;
+    Mt = k.Mt0 + k.Mt1 * h;
+    return rs;
 }
 
-// pass A for an owned cell, plus the centre-only part of pass B: the KKS
-// phase compositions, the parabolas and the driving force dmu
-// (phasefield.c:351-359), so that only (etaS, etaL, c, mu, M, dmu) travel
-// from one plane to the next
-template <typename T>
-__device__ __forceinline__ void pass_a_own(const Coef<T> &k, T eS, T eL, T c, T &mu, T &M, T &dmu) {
-    const T rs = fast_rcp(eS * eS + eL * eL);
-    const T h = eS * eS * rs;
-    const T rA = fast_rcp(k.AS + k.dA * h);
-    mu = k.AsAl * rA * (c - k.cL0 + k.dc0 * h);
-    M = k.ML + k.dM * h;
-    const T cSp = rA * (k.AL * c + (T(1) - h) * k.tmp2);
-    const T cLp = rA * (k.AS * c - h * k.tmp2);
-    const T fS = k.halfAS * (cSp - k.cS0) * (cSp - k.cS0) + k.CS;
-    const T fL = k.halfAL * (cLp - k.cL0) * (cLp - k.cL0) + k.CL;
-    dmu = T(2) * (eS * eL) * (rs * rs) * (fS - fL - mu * (cSp - cLp));
+// pass A for an owned cell plus the centre-only part of pass B: tmp1 dmu
+// of phasefield.c:351-359 through the identity
+//   fS - fL - mu (cS - cL) = (CS-CL) - mu ((cS0-cL0) + (1/AS-1/AL)/2 mu).
+template <typename T, bool EQ>
+__device__ __forceinline__ void pass_a_own(const Coef<T> &k, T eS, T eL, T c, T &mu, T &Mt, T &dmu) {
+    const T rs = pass_a<T, EQ>(k, eS, eL, c, mu, Mt);
+    const T D = EQ ? k.dC - mu * k.q1 : k.dC - mu * (k.q1 + k.q2 * mu);
+    dmu = k.dm2 * (eS * eL) * (rs * rs) * D;
 }
 
 __device__ __forceinline__ void ghosts_of(int i, int n, int bc, int &g0, int &g1) {
@@ -213,7 +210,13 @@ struct ItemWalk {
     __device__ __forceinline__ void advance() { if (++pz > z1) next_item(); }
 };
 
-template <typename T, bool STATS, bool C_ONLY>
+// Registers of the own cells of one plane.
+template <typename T, int CY>
+struct PlaneRegs {
+    T S[CY], L[CY], mu[CY], M[CY], c[CY], d[CY];
+};
+
+template <typename T, bool STATS, bool C_ONLY, bool EQ>
 __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
                     const __grid_constant__ CUtensorMap mapC, Geom g, Coef<T> k, Fields<T> out, int ntx, int nty,
@@ -264,14 +267,12 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
         if (tid == 0)
             for (int l = 0; l < S - 2 && prod.valid(); ++l) issue();
 
-        // registers of the own cells: plane q-1 (p*), plane q (q*), plane q+1 (x*)
-        T pS[CY], pL[CY], pmu[CY], pM[CY];
-        T qS[CY], qL[CY], qmu[CY], qM[CY], qc[CY], qd[CY];
-        T xS[CY], xL[CY], xmu[CY], xM[CY], xc[CY], xd[CY];
+        // three register planes whose roles rotate: q-1, q, q+1
+        PlaneRegs<T, CY> RA, RB, RC;
 #pragma unroll
         for (int j = 0; j < CY; ++j) {
-            pS[j] = pL[j] = pmu[j] = pM[j] = T(0);
-            qS[j] = qL[j] = qmu[j] = qM[j] = qc[j] = qd[j] = T(0);
+            RA.S[j] = RA.L[j] = RA.mu[j] = RA.M[j] = RA.c[j] = RA.d[j] = T(0);
+            RB.S[j] = RB.L[j] = RB.mu[j] = RB.M[j] = RB.c[j] = RB.d[j] = T(0);
         }
 
         ItemWalk cons;
@@ -287,31 +288,32 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             // no own cell of this item touches a domain face in x or y, and all are inside
             const bool inner_xy = x0 > 0 && x0 + TX < g.nx && y0 > 0 && y0 + TY < g.ny;
             const int64_t col = (int64_t)(y0 + ty0 + 1) * g.P + X + g.xoff;   // storage of own cell j=0, z=-1
-            for (int pz = z0 - 1; pz <= z1; ++pz) {
+
+            // one plane: load/pass A of plane pz into Xr, pass B + C of plane pz-1
+            // from (Pr = pz-2, Qr = pz-1, Xr = pz); false once the item is done
+            auto plane = [&](int pz, PlaneRegs<T, CY> &Pr, PlaneRegs<T, CY> &Qr, PlaneRegs<T, CY> &Xr) -> bool {
+                if (pz > z1) return false;
                 if (!mbar_wait(smem_u32(&sm.bar[st]), par, limit_ns)) {
                     sm.abort = 1;
                     atomicOr(err, 1);
                 }
                 const T *rS = sm.raw[st][0], *rL = sm.raw[st][1], *rC = sm.raw[st][2];
                 T *wmu = sm.mm[mb][0], *wM = sm.mm[mb][1];
-                // pass A: own cells into registers and shared memory
 #pragma unroll
                 for (int j = 0; j < CY; ++j) {
                     const int o = ob + j * BX;
-                    xS[j] = rS[o];
-                    xL[j] = rL[o];
-                    xc[j] = rC[o];
+                    Xr.S[j] = rS[o];
+                    Xr.L[j] = rL[o];
+                    Xr.c[j] = rC[o];
                     if (C_ONLY) {
-                        pass_a(k, xS[j], xL[j], xc[j], xmu[j], xM[j]);
-                        xd[j] = T(0);
+                        (void)pass_a<T, EQ>(k, Xr.S[j], Xr.L[j], Xr.c[j], Xr.mu[j], Xr.M[j]);
                     } else {
-                        pass_a_own(k, xS[j], xL[j], xc[j], xmu[j], xM[j], xd[j]);
+                        pass_a_own<T, EQ>(k, Xr.S[j], Xr.L[j], Xr.c[j], Xr.mu[j], Xr.M[j], Xr.d[j]);
                     }
-                    wmu[o] = xmu[j];
-                    wM[o] = xM[j];
+                    wmu[o] = Xr.mu[j];
+                    wM[o] = Xr.M[j];
                 }
-                // pass A: the one-cell ring around the tile
-                if (tid < G::RING) {
+                if (tid < G::RING) {                   // the one-cell ring around the tile
                     int hx, hy;
                     if (tid < TX) { hx = tid; hy = -1; }
                     else if (tid < 2 * TX) { hx = tid - TX; hy = TY; }
@@ -319,15 +321,14 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     else { hx = TX; hy = tid - 2 * TX - TY; }
                     const int o = (hy + 1) * BX + hx + XH;
                     T mu, M;
-                    pass_a(k, rS[o], rL[o], rC[o], mu, M);
+                    (void)pass_a<T, EQ>(k, rS[o], rL[o], rC[o], mu, M);
                     wmu[o] = mu;
                     wM[o] = M;
                 }
                 __syncthreads();
-                if (sm.abort) { dead = true; break; }
+                if (sm.abort) { dead = true; return false; }
                 if (tid == 0 && prod.valid()) issue();   // refill the stage freed two planes ago
 
-                // pass B + C for plane q = pz - 1
                 const int q = pz - 1;
                 if (q >= z0) {
                     const T *nS = sm.raw[st_prev][0], *nL = sm.raw[st_prev][1];
@@ -337,59 +338,65 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
 #pragma unroll
                     for (int j = 0; j < CY; ++j) {
                         const int Y = y0 + ty0 + j;
-                        if (inner || (X < g.nx && Y < g.ny)) {
-                            const int o = ob + j * BX;
-                            const T mu = qmu[j], M = qM[j];
-                            const T muym = j > 0 ? qmu[j - 1] : nmu[o - BX], Mym = j > 0 ? qM[j - 1] : nM[o - BX];
-                            const T muyp = j < CY - 1 ? qmu[j + 1] : nmu[o + BX];
-                            const T Myp = j < CY - 1 ? qM[j + 1] : nM[o + BX];
-                            // solute: flux form of phasefield.c:374-384
-                            const T fl = (xM[j] + M) * (xmu[j] - mu) + (pM[j] + M) * (pmu[j] - mu) +
-                                         (Myp + M) * (muyp - mu) + (Mym + M) * (muym - mu) +
-                                         (nM[o + 1] + M) * (nmu[o + 1] - mu) + (nM[o - 1] + M) * (nmu[o - 1] - mu);
-                            const T dc = k.tmp3 * fl;
-                            const T c = qc[j];
-                            const int64_t a = base + (int64_t)j * g.P;
-                            if (C_ONLY) {
-                                if (inner) out.c[a] = c + dc;
-                                else store_cell<T, true>(g, out, X, Y, q, T(0), T(0), c + dc);
-                                if (STATS) acc[0] += (double)dc * (double)dc;
+                        if (!(inner || (X < g.nx && Y < g.ny))) continue;
+                        const int o = ob + j * BX;
+                        const T mu = Qr.mu[j], M = Qr.M[j], c = Qr.c[j];
+                        const T muym = j > 0 ? Qr.mu[j - 1] : nmu[o - BX], Mym = j > 0 ? Qr.M[j - 1] : nM[o - BX];
+                        const T muyp = j < CY - 1 ? Qr.mu[j + 1] : nmu[o + BX];
+                        const T Myp = j < CY - 1 ? Qr.M[j + 1] : nM[o + BX];
+                        // c + dc: the flux form of phasefield.c:374-384, tmp3 inside M'
+                        T cn = c + (Xr.M[j] + M) * (Xr.mu[j] - mu);
+                        cn += (Pr.M[j] + M) * (Pr.mu[j] - mu);
+                        cn += (Myp + M) * (muyp - mu);
+                        cn += (Mym + M) * (muym - mu);
+                        cn += (nM[o + 1] + M) * (nmu[o + 1] - mu);
+                        cn += (nM[o - 1] + M) * (nmu[o - 1] - mu);
+                        const int64_t a = base + (int64_t)j * g.P;
+                        if (C_ONLY) {
+                            if (inner) out.c[a] = cn;
+                            else store_cell<T, true>(g, out, X, Y, q, T(0), T(0), cn);
+                            if (STATS) {
+                                const double dc = (double)cn - (double)c;
+                                acc[0] += dc * dc;
+                            }
+                        } else {
+                            const T eS = Qr.S[j], eL = Qr.L[j], dmu = Qr.d[j];
+                            const T Sym = j > 0 ? Qr.S[j - 1] : nS[o - BX], Syp = j < CY - 1 ? Qr.S[j + 1] : nS[o + BX];
+                            const T Lym = j > 0 ? Qr.L[j - 1] : nL[o - BX], Lyp = j < CY - 1 ? Qr.L[j + 1] : nL[o + BX];
+                            // detaS, detaL of phasefield.c:360-373 with tmp1 absorbed:
+                            //   eta (mt eta^2 + g2 other^2 + e0) - kt sum6 -/+ other tmp1 dmu
+                            const T S6 = Xr.S[j] + Pr.S[j] + Syp + Sym + nS[o + 1] + nS[o - 1];
+                            const T L6 = Xr.L[j] + Pr.L[j] + Lyp + Lym + nL[o + 1] + nL[o - 1];
+                            const T S2 = eS * eS, L2 = eL * eL;
+                            const T dS = eS * (k.mt * S2 + (k.g2 * L2 + k.e0)) - k.kt * S6 + eL * dmu;
+                            const T dL = eL * (k.mt * L2 + (k.g2 * S2 + k.e0)) - k.kt * L6 - eS * dmu;
+                            if (inner) {
+                                out.eS[a] = eS + dS;
+                                out.eL[a] = eL + dL;
+                                out.c[a] = cn;
                             } else {
-                                const T eS = qS[j], eL = qL[j], dmu = qd[j];
-                                const T Sym = j > 0 ? qS[j - 1] : nS[o - BX], Syp = j < CY - 1 ? qS[j + 1] : nS[o + BX];
-                                const T Lym = j > 0 ? qL[j - 1] : nL[o - BX], Lyp = j < CY - 1 ? qL[j + 1] : nL[o + BX];
-                                // detaS, detaL: phasefield.c:360-373
-                                const T lapS = xS[j] + pS[j] + Syp + Sym + nS[o + 1] + nS[o - 1] - T(6) * eS;
-                                const T lapL = xL[j] + pL[j] + Lyp + Lym + nL[o + 1] + nL[o - 1] - T(6) * eL;
-                                const T dS = k.tmp1 * (k.m * eS * (eS * eS - T(1) + k.twogam * eL * eL) - k.kh2 * lapS + eL * dmu);
-                                const T dL = k.tmp1 * (k.m * eL * (eL * eL - T(1) + k.twogam * eS * eS) - k.kh2 * lapL - eS * dmu);
-                                if (inner) {
-                                    out.eS[a] = eS + dS;
-                                    out.eL[a] = eL + dL;
-                                    out.c[a] = c + dc;
-                                } else {
-                                    store_cell<T, false>(g, out, X, Y, q, eS + dS, eL + dL, c + dc);
-                                }
-                                if (STATS) {
-                                    acc[0] += (double)dc * (double)dc;
-                                    acc[1] += (double)dS * (double)dS;
-                                    acc[2] += (double)dL * (double)dL;
-                                }
+                                store_cell<T, false>(g, out, X, Y, q, eS + dS, eL + dL, cn);
+                            }
+                            if (STATS) {
+                                const double dc = (double)cn - (double)c;
+                                acc[0] += dc * dc;
+                                acc[1] += (double)dS * (double)dS;
+                                acc[2] += (double)dL * (double)dL;
                             }
                         }
                     }
-                }
-#pragma unroll
-                for (int j = 0; j < CY; ++j) {
-                    pS[j] = qS[j]; pL[j] = qL[j]; pmu[j] = qmu[j]; pM[j] = qM[j];
-                    qS[j] = xS[j]; qL[j] = xL[j]; qmu[j] = xmu[j]; qM[j] = xM[j];
-                    qc[j] = xc[j]; qd[j] = xd[j];
                 }
                 st_prev = st;
                 mb_prev = mb;
                 if (++st == S) { st = 0; par ^= 1u; }
                 mb = mb + 1 == 3 ? 0 : mb + 1;
                 ++consumed;
+                return true;
+            };
+            for (int pz = z0 - 1;; pz += 3) {
+                if (!plane(pz, RA, RB, RC)) break;
+                if (!plane(pz + 1, RB, RC, RA)) break;
+                if (!plane(pz + 2, RC, RA, RB)) break;
             }
             if (!dead) cons.next_item();
         }
@@ -453,21 +460,28 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map) {
     return r == CUDA_SUCCESS ? 0 : -3;
 }
 
-template <typename T>
-static cudaError_t set_attrs() {
-    const int bytes = (int)tma_smem_bytes<T>();
-    cudaError_t e;
-    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-        return e;
-    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-        return e;
-    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-        return e;
-    return cudaFuncSetAttribute(step_tma_kernel<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+template <typename T, bool ST, bool CO, bool EQ>
+static cudaError_t set_attr1() {
+    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tma_smem_bytes<T>());
 }
 
-// Launch shape: z chunks of zc planes so that one wave of resident CTAs
-// covers all tiles of consecutive chunks; *zc_out receives the chunk.
+template <typename T>
+static cudaError_t set_attrs() {
+    cudaError_t e;
+    if ((e = set_attr1<T, false, false, false>()) || (e = set_attr1<T, true, false, false>()) ||
+        (e = set_attr1<T, false, true, false>()) || (e = set_attr1<T, true, true, false>()) ||
+        (e = set_attr1<T, false, false, true>()) || (e = set_attr1<T, true, false, true>()) ||
+        (e = set_attr1<T, false, true, true>()) || (e = set_attr1<T, true, true, true>()))
+        return e;
+    return cudaSuccess;
+}
+
+// Launch shape.  Work items are (z chunk, tile) pairs dealt round-robin to
+// a persistent grid of `slots` CTAs (occupancy x SMs).  The chunk length
+// zc is chosen to minimise the busiest CTA's load count -- its planes plus
+// two halo planes per item -- so that the resident CTAs end together;
+// *zc_out receives it.
 template <typename T>
 int tma_grid(const Geom &g, int num_sms, int *zc_out) {
     using G = TmaGeo<T>;
@@ -479,42 +493,60 @@ int tma_grid(const Geom &g, int num_sms, int *zc_out) {
     if (!occ) {
         if (set_attrs<T>() != cudaSuccess) return -1;
         int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false>, G::NT,
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true>, G::NT,
                                                           tma_smem_bytes<T>()) != cudaSuccess || o < 1)
             o = 1;
         occ = o;
     }
     const int64_t ntiles = (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY);
     const int64_t slots = (int64_t)occ * num_sms;
-    // as many chunks as fit one wave, but chunks of at least 8 planes
-    int64_t nc = slots / ntiles;
-    if (nc > g.nz / 8) nc = g.nz / 8;
-    if (nc < 1) nc = 1;
-    const int zc = (int)((g.nz + nc - 1) / nc);
-    nc = (g.nz + zc - 1) / zc;
-    const int64_t items = ntiles * nc;
-    if (items > (int64_t)1 << 30) return -1;
-    *zc_out = zc;
-    return (int)(items < slots ? items : slots);
+    double best_cost = -1;
+    int64_t best_zc = g.nz, best_grid = 1;
+    for (int zc = 1; zc <= g.nz; ++zc) {
+        const int64_t nc = (g.nz + zc - 1) / zc;
+        if (nc > 1 && (nc - 1) * zc >= g.nz) continue;
+        const int64_t items = ntiles * nc;
+        if (items > ((int64_t)1 << 30)) continue;
+        const int64_t grid = items < slots ? items : slots;
+        // items of CTA b: b, b+grid, ...; chunk-major, the last chunk is short
+        const int64_t last = g.nz - (nc - 1) * zc;
+        int64_t worst = 0;
+        for (int64_t b = 0; b < grid; b += (grid > 64 ? grid / 64 : 1)) {
+            int64_t cost = 0;
+            for (int64_t it = b; it < items; it += grid) cost += ((it / ntiles) == nc - 1 ? last : zc) + 2;
+            if (cost > worst) worst = cost;
+        }
+        {   // the final CTA always holds a short item when items % grid != 0
+            int64_t cost = 0;
+            for (int64_t it = grid - 1; it < items; it += grid) cost += ((it / ntiles) == nc - 1 ? last : zc) + 2;
+            if (cost > worst) worst = cost;
+        }
+        // the resident CTAs share the SMs: a wave with fewer CTAs than slots
+        // runs each faster, roughly as slots/grid while memory is the limit
+        const double cost = (double)worst * (grid < slots ? (double)slots / (double)grid : 1.0);
+        if (best_cost < 0 || cost < best_cost) { best_cost = cost; best_zc = zc; best_grid = grid; }
+    }
+    *zc_out = (int)best_zc;
+    return (int)best_grid;
 }
 
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
-                            double *partials, int grid, int zc, int *err, unsigned long long limit_ns, int inject_stall,
-                            cudaStream_t s) {
+                            bool eqA, double *partials, int grid, int zc, int *err, unsigned long long limit_ns,
+                            int inject_stall, cudaStream_t s) {
     using G = TmaGeo<T>;
     const int ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
     const size_t sh = tma_smem_bytes<T>();
     const bool st = partials != nullptr;
-#define PPF_LAUNCH(ST, CO)                                                                                       \
-    step_tma_kernel<T, ST, CO><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty, zc, \
-                                                       partials, err, limit_ns, inject_stall)
-    if (!c_only) {
-        if (st) PPF_LAUNCH(true, false);
-        else PPF_LAUNCH(false, false);
+#define PPF_LAUNCH(ST, CO, EQ)                                                                                   \
+    step_tma_kernel<T, ST, CO, EQ><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty, zc,  \
+                                                           partials, err, limit_ns, inject_stall)
+    if (eqA) {
+        if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
+        else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
     } else {
-        if (st) PPF_LAUNCH(true, true);
-        else PPF_LAUNCH(false, true);
+        if (!c_only) { if (st) PPF_LAUNCH(true, false, false); else PPF_LAUNCH(false, false, false); }
+        else { if (st) PPF_LAUNCH(true, true, false); else PPF_LAUNCH(false, true, false); }
     }
 #undef PPF_LAUNCH
     return cudaGetLastError();
@@ -525,9 +557,10 @@ template int make_field_map<double>(const Geom &, const double *, CUtensorMap *)
 template int tma_grid<float>(const Geom &, int, int *);
 template int tma_grid<double>(const Geom &, int, int *);
 template cudaError_t launch_step_tma<float>(const Geom &, const Coef<float> &, const CUtensorMap *, Fields<float>,
-                                            bool, double *, int, int, int *, unsigned long long, int, cudaStream_t);
+                                            bool, bool, double *, int, int, int *, unsigned long long, int,
+                                            cudaStream_t);
 template cudaError_t launch_step_tma<double>(const Geom &, const Coef<double> &, const CUtensorMap *,
-                                             Fields<double>, bool, double *, int, int, int *, unsigned long long, int,
-                                             cudaStream_t);
+                                             Fields<double>, bool, bool, double *, int, int, int *, unsigned long long,
+                                             int, cudaStream_t);
 
 }  // namespace ppf

@@ -18,13 +18,14 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map);
 template <typename T>
 int tma_grid(const Geom &g, int num_sms, int *zc);
 
-// One fused step.  maps = {etaS, etaL, c} of the input state; `partials`
+// One fused step.  maps = {etaS, etaL, c} of the input state; eqA selects
+// the specialisation for AS == AL (mu needs no reciprocal); `partials`
 // (nullable) receives 3 doubles per CTA; `err` is a device word that a
 // CTA sets when an mbarrier wait exceeds limit_ns.  inject_stall != 0 is a
 // test hook that makes one wait per CTA run out.
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
-                            double *partials, int grid, int zc, int *err, unsigned long long limit_ns,
+                            bool eqA, double *partials, int grid, int zc, int *err, unsigned long long limit_ns,
                             int inject_stall, cudaStream_t s);
 
 }  // namespace ppf

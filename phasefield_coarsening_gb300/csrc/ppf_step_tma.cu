@@ -344,21 +344,21 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                         const T muym = j > 0 ? Qr.mu[j - 1] : nmu[o - BX], Mym = j > 0 ? Qr.M[j - 1] : nM[o - BX];
                         const T muyp = j < CY - 1 ? Qr.mu[j + 1] : nmu[o + BX];
                         const T Myp = j < CY - 1 ? Qr.M[j + 1] : nM[o + BX];
-                        // c + dc: the flux form of phasefield.c:374-384, tmp3 inside M'
-                        T cn = c + (Xr.M[j] + M) * (Xr.mu[j] - mu);
-                        cn += (Pr.M[j] + M) * (Pr.mu[j] - mu);
-                        cn += (Myp + M) * (muyp - mu);
-                        cn += (Mym + M) * (muym - mu);
-                        cn += (nM[o + 1] + M) * (nmu[o + 1] - mu);
-                        cn += (nM[o - 1] + M) * (nmu[o - 1] - mu);
+                        // dc: the flux form of phasefield.c:374-384, tmp3 inside M'.
+                        // The six face fluxes are summed first and added to c once,
+                        // so c is rounded once per step.
+                        T fl = (Xr.M[j] + M) * (Xr.mu[j] - mu);
+                        fl += (Pr.M[j] + M) * (Pr.mu[j] - mu);
+                        fl += (Myp + M) * (muyp - mu);
+                        fl += (Mym + M) * (muym - mu);
+                        fl += (nM[o + 1] + M) * (nmu[o + 1] - mu);
+                        fl += (nM[o - 1] + M) * (nmu[o - 1] - mu);
+                        const T cn = c + fl;
                         const int64_t a = base + (int64_t)j * g.P;
                         if (C_ONLY) {
                             if (inner) out.c[a] = cn;
                             else store_cell<T, true>(g, out, X, Y, q, T(0), T(0), cn);
-                            if (STATS) {
-                                const double dc = (double)cn - (double)c;
-                                acc[0] += dc * dc;
-                            }
+                            if (STATS) acc[0] += (double)fl * (double)fl;
                         } else {
                             const T eS = Qr.S[j], eL = Qr.L[j], dmu = Qr.d[j];
                             const T Sym = j > 0 ? Qr.S[j - 1] : nS[o - BX], Syp = j < CY - 1 ? Qr.S[j + 1] : nS[o + BX];
@@ -378,8 +378,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                                 store_cell<T, false>(g, out, X, Y, q, eS + dS, eL + dL, cn);
                             }
                             if (STATS) {
-                                const double dc = (double)cn - (double)c;
-                                acc[0] += dc * dc;
+                                acc[0] += (double)fl * (double)fl;
                                 acc[1] += (double)dS * (double)dS;
                                 acc[2] += (double)dL * (double)dL;
                             }

@@ -122,7 +122,13 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map
 template <typename T>
 __device__ __forceinline__ T fast_rcp(T x);
 template <>
-__device__ __forceinline__ float fast_rcp<float>(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ float fast_rcp<float>(float x) {
+    // the hardware reciprocal (rcp.approx.ftz.f32, ~1 ulp): the operands are
+    // sums of squares and interpolation weights, never denormal or huge
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 template <>
 __device__ __forceinline__ double fast_rcp<double>(double x) { return __drcp_rn(x); }
 
@@ -167,9 +173,10 @@ __device__ __forceinline__ void put(const Geom &g, const Fields<T> &o, int64_t i
     o.c[i] = c;
 }
 
-// the new state of cell (x,y,z) and every face ghost that mirrors it
+// the new state of cell (x,y,z) and every face ghost that mirrors it (kept
+// out of line: only tiles on a domain face take this path)
 template <typename T, bool C_ONLY>
-__device__ __forceinline__ void store_cell(const Geom &g, const Fields<T> &o, int x, int y, int z, T s, T l, T c) {
+__device__ __noinline__ void store_cell(const Geom &g, const Fields<T> &o, int x, int y, int z, T s, T l, T c) {
     put<T, C_ONLY>(g, o, g.at(x, y, z), s, l, c);
     if (x == 0 || y == 0 || z == 0 || x == g.nx - 1 || y == g.ny - 1 || z == g.nz - 1) {
         int a, b;
@@ -224,8 +231,12 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     int inject_stall) {
     using G = TmaGeo<T>;
     constexpr int TX = G::TX, TY = G::TY, S = G::S, XH = G::XH, BX = G::BX, CY = G::CY;
-    extern __shared__ unsigned char smem_dyn[];
-    TmaSmem<T> &sm = *reinterpret_cast<TmaSmem<T> *>((reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~uintptr_t(127));
+    extern __shared__ __align__(128) unsigned char smem_dyn[];
+    // 128-byte alignment by an offset from the shared array itself, so that
+    // every derived pointer stays a shared-window pointer (LDS/STS, 32-bit
+    // addressing) rather than a generic one
+    const uint32_t pad = (128u - (smem_u32(smem_dyn) & 127u)) & 127u;
+    TmaSmem<T> &sm = *reinterpret_cast<TmaSmem<T> *>(smem_dyn + pad);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = (warp % G::WX) * 32 + lane;        // own column in the tile

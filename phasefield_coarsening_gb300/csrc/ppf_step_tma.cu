@@ -157,38 +157,30 @@ __device__ __forceinline__ void pass_a_own(const Coef<T> &k, T eS, T eL, T c, T 
     dmu = k.dm2 * (eS * eL) * (rs * rs) * D;
 }
 
-__device__ __forceinline__ void ghosts_of(int i, int n, int bc, int &g0, int &g1) {
-    g0 = -2;
-    g1 = -2;
-    if (i == 0) g0 = (bc == 0) ? n : -1;
-    if (i == n - 1) g1 = (bc == 0) ? -1 : n;
-}
-
+// Face ghosts fed by a boundary cell (the BC fill of phasefield.c:1112-1189
+// applied to the new state): along an axis of n cells and stride st, cell 0
+// is copied to ghost n (periodic) or -1 (no-flux), cell n-1 to ghost -1
+// (periodic) or n (no-flux).  `a` is the cell's own storage index; each
+// ghost is an offset from it.
 template <typename T, bool C_ONLY>
-__device__ __forceinline__ void put(const Geom &g, const Fields<T> &o, int64_t i, T s, T l, T c) {
+__device__ __forceinline__ void put_ghost(const Fields<T> &o, int64_t a, T s, T l, T c) {
     if (!C_ONLY) {
-        o.eS[i] = s;
-        o.eL[i] = l;
+        o.eS[a] = s;
+        o.eL[a] = l;
     }
-    o.c[i] = c;
+    o.c[a] = c;
 }
 
-// the new state of cell (x,y,z) and every face ghost that mirrors it (kept
-// out of line: only tiles on a domain face take this path)
 template <typename T, bool C_ONLY>
-__device__ __noinline__ void store_cell(const Geom &g, const Fields<T> &o, int x, int y, int z, T s, T l, T c) {
-    put<T, C_ONLY>(g, o, g.at(x, y, z), s, l, c);
-    if (x == 0 || y == 0 || z == 0 || x == g.nx - 1 || y == g.ny - 1 || z == g.nz - 1) {
-        int a, b;
-        ghosts_of(x, g.nx, g.bc, a, b);
-        if (a != -2) put<T, C_ONLY>(g, o, g.at(a, y, z), s, l, c);
-        if (b != -2) put<T, C_ONLY>(g, o, g.at(b, y, z), s, l, c);
-        ghosts_of(y, g.ny, g.bc, a, b);
-        if (a != -2) put<T, C_ONLY>(g, o, g.at(x, a, z), s, l, c);
-        if (b != -2) put<T, C_ONLY>(g, o, g.at(x, b, z), s, l, c);
-        ghosts_of(z, g.nz, g.bc, a, b);
-        if (a != -2) put<T, C_ONLY>(g, o, g.at(x, y, a), s, l, c);
-        if (b != -2) put<T, C_ONLY>(g, o, g.at(x, y, b), s, l, c);
+__device__ __forceinline__ void store_ghosts(const Geom &g, const Fields<T> &o, int64_t a, int x, int y, int z, T s,
+                                             T l, T c) {
+    const int idx[3] = {x, y, z};
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const int64_t st[3] = {1, g.P, g.PS};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (idx[d] == 0) put_ghost<T, C_ONLY>(o, a + (g.bc == 0 ? (int64_t)n[d] : (int64_t)-1) * st[d], s, l, c);
+        if (idx[d] == n[d] - 1) put_ghost<T, C_ONLY>(o, a + (g.bc == 0 ? -(int64_t)n[d] : (int64_t)1) * st[d], s, l, c);
     }
 }
 
@@ -296,8 +288,14 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             const int bx = cons.tile % ntx, by = cons.tile / ntx;
             const int x0 = bx * TX, y0 = by * TY, z0 = cons.z0, z1 = cons.z1;
             const int X = x0 + tx;
-            // no own cell of this item touches a domain face in x or y, and all are inside
-            const bool inner_xy = x0 > 0 && x0 + TX < g.nx && y0 > 0 && y0 + TY < g.ny;
+            // per own row j: inside the domain (bit j of vmask), on an x or y face (bit j of emask)
+            unsigned vmask = 0, emask = 0;
+#pragma unroll
+            for (int j = 0; j < CY; ++j) {
+                const int Y = y0 + ty0 + j;
+                if (X < g.nx && Y < g.ny) vmask |= 1u << j;
+                if (X == 0 || X == g.nx - 1 || Y == 0 || Y == g.ny - 1) emask |= 1u << j;
+            }
             const int64_t col = (int64_t)(y0 + ty0 + 1) * g.P + X + g.xoff;   // storage of own cell j=0, z=-1
 
             // one plane: load/pass A of plane pz into Xr, pass B + C of plane pz-1
@@ -344,12 +342,12 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 if (q >= z0) {
                     const T *nS = sm.raw[st_prev][0], *nL = sm.raw[st_prev][1];
                     const T *nmu = sm.mm[mb_prev][0], *nM = sm.mm[mb_prev][1];
-                    const bool inner = inner_xy && q > 0 && q < g.nz - 1;
+                    const bool zface = q == 0 || q == g.nz - 1;
                     const int64_t base = col + (int64_t)(q + 1) * g.PS;
 #pragma unroll
                     for (int j = 0; j < CY; ++j) {
-                        const int Y = y0 + ty0 + j;
-                        if (!(inner || (X < g.nx && Y < g.ny))) continue;
+                        if (!(vmask & (1u << j))) continue;
+                        const bool edge = zface || (emask & (1u << j));
                         const int o = ob + j * BX;
                         const T mu = Qr.mu[j], M = Qr.M[j], c = Qr.c[j];
                         const T muym = j > 0 ? Qr.mu[j - 1] : nmu[o - BX], Mym = j > 0 ? Qr.M[j - 1] : nM[o - BX];
@@ -367,8 +365,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                         const T cn = c + fl;
                         const int64_t a = base + (int64_t)j * g.P;
                         if (C_ONLY) {
-                            if (inner) out.c[a] = cn;
-                            else store_cell<T, true>(g, out, X, Y, q, T(0), T(0), cn);
+                            out.c[a] = cn;
+                            if (edge) store_ghosts<T, true>(g, out, a, X, y0 + ty0 + j, q, T(0), T(0), cn);
                             if (STATS) acc[0] += (double)fl * (double)fl;
                         } else {
                             const T eS = Qr.S[j], eL = Qr.L[j], dmu = Qr.d[j];
@@ -381,13 +379,10 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             const T S2 = eS * eS, L2 = eL * eL;
                             const T dS = eS * (k.mt * S2 + (k.g2 * L2 + k.e0)) - k.kt * S6 + eL * dmu;
                             const T dL = eL * (k.mt * L2 + (k.g2 * S2 + k.e0)) - k.kt * L6 - eS * dmu;
-                            if (inner) {
-                                out.eS[a] = eS + dS;
-                                out.eL[a] = eL + dL;
-                                out.c[a] = cn;
-                            } else {
-                                store_cell<T, false>(g, out, X, Y, q, eS + dS, eL + dL, cn);
-                            }
+                            out.eS[a] = eS + dS;
+                            out.eL[a] = eL + dL;
+                            out.c[a] = cn;
+                            if (edge) store_ghosts<T, false>(g, out, a, X, y0 + ty0 + j, q, eS + dS, eL + dL, cn);
                             if (STATS) {
                                 acc[0] += (double)fl * (double)fl;
                                 acc[1] += (double)dS * (double)dS;

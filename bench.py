@@ -174,6 +174,7 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     sim.set_stream(stream.cuda_stream)
     sim.upload(eS, eL, c)
+    tune = sim.autotune(trial_steps=10)        # the project's launch autotuner (state is kept)
 
     def bench_step():
         sim.step(INNER)
@@ -247,11 +248,12 @@ def run_ours(args):
                     f"{info['sphere_fraction']:.3f}), generated on the host",
             "config": {"workload": WORKLOAD, "grid": list(shape), "bc": "periodic", "dt": DT,
                        "time_steps_per_bench_step": INNER, "precision": "f32 storage and arithmetic, FP64 reductions",
-                       "l2": "state 403 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+                       "l2": "state 403 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas x{world}",
+                       "launch": {"zc": tune["zc"], "roll": tune["roll"], "grid": tune["grid"]}},
             "sim_time_per_wall_s": round(value * 1e9 / cells * DT, 1),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(achieved / hbm, 4), "traffic": traffic,
-                         "kernel": "step_kernel<float,64,8,256>", "algorithmic_bytes_per_launch": ALG_BYTES_F32 * cells,
+                         "kernel": "step_tma_kernel<float> (fused step, TMA-fed)", "algorithmic_bytes_per_launch": ALG_BYTES_F32 * cells,
                          "avg_launch_us": round(step_ms * 1e3, 2), "peak_source": src},
             "e2e": {"value": round(e2e_value, 3), "unit": "GLUPS", "h2d_bytes_per_step": 3 * cells * 8,
                     "d2h_bytes_per_step": 3 * cells * 8 + 8 * 8},

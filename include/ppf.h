@@ -162,6 +162,25 @@ int ppf_set_wait_limit(ppf_ctx *ctx, double seconds);
 #define PPF_INJECT_STALL_WAIT 1
 int ppf_debug_inject(ppf_ctx *ctx, int fault);
 
+/* Launch choices of the fused step kernel.  No counterpart in the
+ * reference (whose only tuning is the no-op cache blocking of
+ * phasefield.c:58-62, :340-350). */
+typedef struct ppf_tune {
+    int zc;              /* z planes per work item of the persistent grid */
+    int roll;            /* 3: plane body unrolled three times, 1: one copy */
+    int grid;            /* CTAs (derived from zc; ignored by ppf_set_tune) */
+    double us_per_step;  /* measured time of the winner (ppf_autotune only) */
+} ppf_tune;
+
+int ppf_get_tune(const ppf_ctx *ctx, ppf_tune *out);
+int ppf_set_tune(ppf_ctx *ctx, const ppf_tune *t);
+
+/* Time the candidate launch choices on the context's uploaded state for
+ * `trial_steps` steps each, keep the fastest, and restore the state as it
+ * was (the step count is unchanged).  `best` (may be NULL) receives the
+ * choice and its time per step. */
+int ppf_autotune(ppf_ctx *ctx, int trial_steps, ppf_tune *best);
+
 /* Message for the calling thread's last failure ("" if none). */
 const char *ppf_last_error(void);
 

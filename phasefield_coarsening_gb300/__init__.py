@@ -27,7 +27,8 @@ _PREC = {"f64": F64, "f32": F32, F64: F64, F32: F32}
 EXPORTS = (
     "ppf_params_default", "ppf_params_derive", "ppf_create", "ppf_destroy", "ppf_get_dims", "ppf_set_stream",
     "ppf_upload", "ppf_download", "ppf_upload_device", "ppf_download_device", "ppf_step", "ppf_step_c_only",
-    "ppf_reduce", "ppf_sync", "ppf_set_wait_limit", "ppf_debug_inject", "ppf_last_error", "ppf_version",
+    "ppf_reduce", "ppf_sync", "ppf_set_wait_limit", "ppf_debug_inject", "ppf_get_tune", "ppf_set_tune",
+    "ppf_autotune", "ppf_last_error", "ppf_version",
     "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_last_error",
 )
 
@@ -54,6 +55,14 @@ class Stats(ctypes.Structure):
                 ("mass", ctypes.c_double), ("solid", ctypes.c_double), ("solid_cells", ctypes.c_double),
                 ("free_energy", ctypes.c_double), ("cells", ctypes.c_int64), ("nonfinite", ctypes.c_int64),
                 ("steps", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Tune(ctypes.Structure):
+    """ppf_tune: launch choices of the fused step."""
+    _fields_ = [("zc", ctypes.c_int), ("roll", ctypes.c_int), ("grid", ctypes.c_int), ("us_per_step", ctypes.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -92,6 +101,9 @@ def lib() -> ctypes.CDLL:
         L.ppf_reduce.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
         L.ppf_set_wait_limit.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.ppf_debug_inject.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ppf_get_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
+        L.ppf_set_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
+        L.ppf_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Tune)]
         L.ppf_get_dims.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 3
         L.ppf_h5_dims.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.ppf_h5_read3d.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _dp,
@@ -197,6 +209,20 @@ class Simulation:
 
     def debug_inject(self, fault: int):
         _check(lib().ppf_debug_inject(self._h, int(fault)))
+
+    def get_tune(self) -> dict:
+        t = Tune()
+        _check(lib().ppf_get_tune(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tune(self, zc: int, roll: int = 3):
+        t = Tune(int(zc), int(roll), 0, 0.0)
+        _check(lib().ppf_set_tune(self._h, ctypes.byref(t)))
+
+    def autotune(self, trial_steps: int = 10) -> dict:
+        t = Tune()
+        _check(lib().ppf_autotune(self._h, int(trial_steps), ctypes.byref(t)))
+        return t.as_dict()
 
     def reduce(self) -> dict:
         s = Stats()

@@ -54,8 +54,7 @@ struct ppf_ctx {
     double *dres;         // device results: [0..2] increments, [3..7] observables
     int *derr;            // device error word set by a kernel whose bounded wait ran out
     CUtensorMap maps[2][3];   // TMA maps of the fields of both buffers
-    int grid;             // persistent grid of the fused step
-    int zc;               // z chunk of one work item
+    StepTune tune;        // launch choices of the fused step (grid, z chunk, unroll)
     unsigned long long wait_limit_ns;
     int inject;           // test hook: PPF_INJECT_*
     int64_t steps;
@@ -213,9 +212,10 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
                 return seterr(PPF_ECUDA, "TMA descriptor setup failed (%d)", mr);
             }
         }
-    c->grid = precision == PPF_F32 ? tma_grid<float>(c->g, c->num_sms, &c->zc)
-                                   : tma_grid<double>(c->g, c->num_sms, &c->zc);
-    if (c->grid < 1) {
+    c->tune.roll = 3;
+    c->tune.grid = precision == PPF_F32 ? tma_grid<float>(c->g, c->num_sms, &c->tune.zc)
+                                        : tma_grid<double>(c->g, c->num_sms, &c->tune.zc);
+    if (c->tune.grid < 1) {
         ppf_destroy(c);
         return seterr(PPF_ECUDA, "kernel attribute setup failed");
     }
@@ -346,7 +346,7 @@ static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
     if (nsteps < 0) return seterr(PPF_EINVAL, "negative step count");
     if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
     if (nsteps == 0) return PPF_OK;
-    int rc = ensure_partials(c, 3 * c->grid);
+    int rc = ensure_partials(c, 3 * c->tune.grid);
     if (rc) return rc;
     for (int64_t s = 0; s < nsteps; ++s) {
         const bool last = s == nsteps - 1;
@@ -358,18 +358,18 @@ static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
         cudaError_t e;
         if (c->prec == PPF_F32) {
             const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
-            e = launch_step_tma<float>(c->g, c->kf, m, ff(c, oe, oc), c_only, c->eqA, part, c->grid,
-                                       c->zc, c->derr, c->wait_limit_ns, inject, c->stream);
+            e = launch_step_tma<float>(c->g, c->kf, m, ff(c, oe, oc), c_only, c->eqA, part, c->tune,
+                                       c->derr, c->wait_limit_ns, inject, c->stream);
         } else {
             const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
-            e = launch_step_tma<double>(c->g, c->kd, m, fd(c, oe, oc), c_only, c->eqA, part, c->grid,
-                                        c->zc, c->derr, c->wait_limit_ns, inject, c->stream);
+            e = launch_step_tma<double>(c->g, c->kd, m, fd(c, oe, oc), c_only, c->eqA, part, c->tune,
+                                        c->derr, c->wait_limit_ns, inject, c->stream);
         }
         if (e != cudaSuccess) return seterr(PPF_ECUDA, "step launch failed: %s", cudaGetErrorString(e));
         c->cur_eta = oe;
         c->cur_c = oc;
         c->steps++;
-        if (last) CU(launch_final_sum(c->partials, c->grid, 3, c_only ? 1 : 3, c->dres, c->stream));
+        if (last) CU(launch_final_sum(c->partials, c->tune.grid, 3, c_only ? 1 : 3, c->dres, c->stream));
     }
     return PPF_OK;
 }
@@ -426,6 +426,100 @@ extern "C" int ppf_debug_inject(ppf_ctx *c, int fault) {
     if (!c) return seterr(PPF_EINVAL, "null context");
     if (fault != PPF_INJECT_NONE && fault != PPF_INJECT_STALL_WAIT) return seterr(PPF_EINVAL, "unknown fault %d", fault);
     c->inject = fault;
+    return PPF_OK;
+}
+
+static int grid_for(ppf_ctx *c, int zc) {
+    return c->prec == PPF_F32 ? tma_grid_for_zc<float>(c->g, c->num_sms, zc)
+                              : tma_grid_for_zc<double>(c->g, c->num_sms, zc);
+}
+
+extern "C" int ppf_get_tune(const ppf_ctx *c, ppf_tune *t) {
+    if (!c || !t) return seterr(PPF_EINVAL, "null argument");
+    t->zc = c->tune.zc;
+    t->roll = c->tune.roll;
+    t->grid = c->tune.grid;
+    t->us_per_step = 0.0;
+    return PPF_OK;
+}
+
+extern "C" int ppf_set_tune(ppf_ctx *c, const ppf_tune *t) {
+    if (!c || !t) return seterr(PPF_EINVAL, "null argument");
+    if (t->roll != 1 && t->roll != 3) return seterr(PPF_EINVAL, "roll must be 1 or 3");
+    if (t->zc < 1 || t->zc > c->nz) return seterr(PPF_EINVAL, "zc must be in [1, nz]");
+    CU(cudaStreamSynchronize(c->stream));
+    const int grid = grid_for(c, t->zc);
+    if (grid < 1) return seterr(PPF_ECUDA, "no launch shape for zc=%d", t->zc);
+    c->tune.zc = t->zc;
+    c->tune.roll = t->roll;
+    c->tune.grid = grid;
+    return PPF_OK;
+}
+
+extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
+    if (!c) return seterr(PPF_EINVAL, "null context");
+    if (!c->uploaded) return seterr(PPF_ESTATE, "autotuning needs an uploaded state");
+    if (trial_steps < 1) trial_steps = 1;
+    // candidates: the model's chunk, powers of two, a single chunk; both unrolls
+    int zcs[16], nzc = 0;
+    auto add = [&](int z) {
+        if (z < 1 || z > c->nz) return;
+        for (int i = 0; i < nzc; ++i)
+            if (zcs[i] == z) return;
+        if (nzc < 16) zcs[nzc++] = z;
+    };
+    add(c->tune.zc);
+    add(c->nz);
+    for (int z = 8; z <= 128; z *= 2) add(z);
+    add((c->tune.zc + 1) / 2);
+    add(c->tune.zc * 2);
+    // keep the state: the trials advance it, so save it and restore it after
+    const int64_t steps0 = c->steps;
+    int rc = do_unpack(c);
+    if (rc) return rc;
+    const StepTune keep = c->tune;
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    float best_ms = -1.0f;
+    StepTune win = keep;
+    for (int r = 0; r < 2 && rc == PPF_OK; ++r)
+        for (int i = 0; i < nzc && rc == PPF_OK; ++i) {
+            StepTune t;
+            t.roll = r == 0 ? 3 : 1;
+            t.zc = zcs[i];
+            t.grid = grid_for(c, t.zc);
+            if (t.grid < 1) continue;
+            c->tune = t;
+            if ((rc = run_steps(c, 2, false)) != PPF_OK) break;      // warm-up
+            if (cudaEventRecord(e0, c->stream) != cudaSuccess) { rc = seterr(PPF_ECUDA, "event record"); break; }
+            if ((rc = run_steps(c, trial_steps, false)) != PPF_OK) break;
+            if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = seterr(PPF_ECUDA, "event timing failed");
+                break;
+            }
+            if ((rc = check_device_error(c)) != PPF_OK) break;
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (best_ms < 0 || ms < best_ms) { best_ms = ms; win = t; }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->tune = rc == PPF_OK ? win : keep;
+    int rc2 = do_pack(c);           // restore the state saved above
+    c->steps = steps0;
+    if (rc2 == PPF_OK) {
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) rc2 = seterr(PPF_ECUDA, "restore failed: %s", cudaGetErrorString(e));
+    }
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (best) {
+        best->zc = win.zc;
+        best->roll = win.roll;
+        best->grid = win.grid;
+        best->us_per_step = best_ms * 1000.0 / trial_steps;
+    }
     return PPF_OK;
 }
 

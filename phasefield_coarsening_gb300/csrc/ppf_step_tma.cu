@@ -215,7 +215,7 @@ struct PlaneRegs {
     T S[CY], L[CY], mu[CY], M[CY], c[CY], d[CY];
 };
 
-template <typename T, bool STATS, bool C_ONLY, bool EQ>
+template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL>
 __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
                     const __grid_constant__ CUtensorMap mapC, Geom g, Coef<T> k, Fields<T> out, int ntx, int nty,
@@ -347,7 +347,6 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
 #pragma unroll
                     for (int j = 0; j < CY; ++j) {
                         if (!(vmask & (1u << j))) continue;
-                        const bool edge = zface || (emask & (1u << j));
                         const int o = ob + j * BX;
                         const T mu = Qr.mu[j], M = Qr.M[j], c = Qr.c[j];
                         const T muym = j > 0 ? Qr.mu[j - 1] : nmu[o - BX], Mym = j > 0 ? Qr.M[j - 1] : nM[o - BX];
@@ -366,7 +365,6 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                         const int64_t a = base + (int64_t)j * g.P;
                         if (C_ONLY) {
                             out.c[a] = cn;
-                            if (edge) store_ghosts<T, true>(g, out, a, X, y0 + ty0 + j, q, T(0), T(0), cn);
                             if (STATS) acc[0] += (double)fl * (double)fl;
                         } else {
                             const T eS = Qr.S[j], eL = Qr.L[j], dmu = Qr.d[j];
@@ -382,12 +380,25 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             out.eS[a] = eS + dS;
                             out.eL[a] = eL + dL;
                             out.c[a] = cn;
-                            if (edge) store_ghosts<T, false>(g, out, a, X, y0 + ty0 + j, q, eS + dS, eL + dL, cn);
                             if (STATS) {
                                 acc[0] += (double)fl * (double)fl;
                                 acc[1] += (double)dS * (double)dS;
                                 acc[2] += (double)dL * (double)dL;
                             }
+                        }
+                    }
+                    // face ghosts of this thread's boundary cells: read back the
+                    // values it just stored (own writes, program order) and copy
+                    // them to the ghosts; one compact loop instead of a copy per cell
+                    const unsigned gm = vmask & (zface ? ~0u : emask);
+                    if (gm) {
+#pragma unroll 1
+                        for (int j = 0; j < CY; ++j) {
+                            if (!(gm & (1u << j))) continue;
+                            const int64_t a = base + (int64_t)j * g.P;
+                            const T c = out.c[a];
+                            const T sv = C_ONLY ? T(0) : out.eS[a], lv = C_ONLY ? T(0) : out.eL[a];
+                            store_ghosts<T, C_ONLY>(g, out, a, X, y0 + ty0 + j, q, sv, lv, c);
                         }
                     }
                 }
@@ -398,10 +409,22 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 ++consumed;
                 return true;
             };
-            for (int pz = z0 - 1;; pz += 3) {
-                if (!plane(pz, RA, RB, RC)) break;
-                if (!plane(pz + 1, RB, RC, RA)) break;
-                if (!plane(pz + 2, RC, RA, RB)) break;
+            if (ROLL == 3) {
+                // three copies of the plane body, the register planes renamed
+                // instead of copied
+                for (int pz = z0 - 1;; pz += 3) {
+                    if (!plane(pz, RA, RB, RC)) break;
+                    if (!plane(pz + 1, RB, RC, RA)) break;
+                    if (!plane(pz + 2, RC, RA, RB)) break;
+                }
+            } else {
+                // one copy of the plane body (a third of the code), the
+                // register planes moved down after each plane
+                for (int pz = z0 - 1;; ++pz) {
+                    if (!plane(pz, RA, RB, RC)) break;
+                    RA = RB;
+                    RB = RC;
+                }
             }
             if (!dead) cons.next_item();
         }
@@ -465,21 +488,27 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map) {
     return r == CUDA_SUCCESS ? 0 : -3;
 }
 
-template <typename T, bool ST, bool CO, bool EQ>
+template <typename T, bool ST, bool CO, bool EQ, int R>
 static cudaError_t set_attr1() {
-    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)tma_smem_bytes<T>());
+}
+
+template <typename T, int R>
+static cudaError_t set_attrs_r() {
+    cudaError_t e;
+    if ((e = set_attr1<T, false, false, false, R>()) || (e = set_attr1<T, true, false, false, R>()) ||
+        (e = set_attr1<T, false, true, false, R>()) || (e = set_attr1<T, true, true, false, R>()) ||
+        (e = set_attr1<T, false, false, true, R>()) || (e = set_attr1<T, true, false, true, R>()) ||
+        (e = set_attr1<T, false, true, true, R>()) || (e = set_attr1<T, true, true, true, R>()))
+        return e;
+    return cudaSuccess;
 }
 
 template <typename T>
 static cudaError_t set_attrs() {
-    cudaError_t e;
-    if ((e = set_attr1<T, false, false, false>()) || (e = set_attr1<T, true, false, false>()) ||
-        (e = set_attr1<T, false, true, false>()) || (e = set_attr1<T, true, true, false>()) ||
-        (e = set_attr1<T, false, false, true>()) || (e = set_attr1<T, true, false, true>()) ||
-        (e = set_attr1<T, false, true, true>()) || (e = set_attr1<T, true, true, true>()))
-        return e;
-    return cudaSuccess;
+    cudaError_t e = set_attrs_r<T, 1>();
+    return e ? e : set_attrs_r<T, 3>();
 }
 
 // Launch shape.  Work items are (z chunk, tile) pairs dealt round-robin to
@@ -498,7 +527,7 @@ int tma_grid(const Geom &g, int num_sms, int *zc_out) {
     if (!occ) {
         if (set_attrs<T>() != cudaSuccess) return -1;
         int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true>, G::NT,
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 3>, G::NT,
                                                           tma_smem_bytes<T>()) != cudaSuccess || o < 1)
             o = 1;
         occ = o;
@@ -536,16 +565,34 @@ int tma_grid(const Geom &g, int num_sms, int *zc_out) {
 }
 
 template <typename T>
-cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
-                            bool eqA, double *partials, int grid, int zc, int *err, unsigned long long limit_ns,
-                            int inject_stall, cudaStream_t s) {
+int tma_grid_for_zc(const Geom &g, int num_sms, int zc) {
+    using G = TmaGeo<T>;
+    int dummy = 0;
+    if (tma_grid<T>(g, num_sms, &dummy) < 1) return -1;    // attributes + occupancy
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 3>, G::NT,
+                                                      tma_smem_bytes<T>()) != cudaSuccess || occ < 1)
+        occ = 1;
+    const int64_t ntiles = (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY);
+    if (zc < 1) zc = 1;
+    if (zc > g.nz) zc = g.nz;
+    const int64_t items = ntiles * ((g.nz + zc - 1) / zc);
+    const int64_t slots = (int64_t)occ * num_sms;
+    if (items > ((int64_t)1 << 30)) return -1;
+    return (int)(items < slots ? items : slots);
+}
+
+template <typename T, int R>
+static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only, bool eqA,
+                     double *partials, int grid, int zc, int *err, unsigned long long limit_ns, int inject_stall,
+                     cudaStream_t s) {
     using G = TmaGeo<T>;
     const int ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
     const size_t sh = tma_smem_bytes<T>();
     const bool st = partials != nullptr;
-#define PPF_LAUNCH(ST, CO, EQ)                                                                                   \
-    step_tma_kernel<T, ST, CO, EQ><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty, zc,  \
-                                                           partials, err, limit_ns, inject_stall)
+#define PPF_LAUNCH(ST, CO, EQ)                                                                                      \
+    step_tma_kernel<T, ST, CO, EQ, R><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty, zc, \
+                                                              partials, err, limit_ns, inject_stall)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -554,6 +601,16 @@ cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *
         else { if (st) PPF_LAUNCH(true, true, false); else PPF_LAUNCH(false, true, false); }
     }
 #undef PPF_LAUNCH
+}
+
+template <typename T>
+cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
+                            bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
+                            int inject_stall, cudaStream_t s) {
+    if (tune.roll == 1)
+        launch_r<T, 1>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns, inject_stall, s);
+    else
+        launch_r<T, 3>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns, inject_stall, s);
     return cudaGetLastError();
 }
 
@@ -561,11 +618,13 @@ template int make_field_map<float>(const Geom &, const float *, CUtensorMap *);
 template int make_field_map<double>(const Geom &, const double *, CUtensorMap *);
 template int tma_grid<float>(const Geom &, int, int *);
 template int tma_grid<double>(const Geom &, int, int *);
+template int tma_grid_for_zc<float>(const Geom &, int, int);
+template int tma_grid_for_zc<double>(const Geom &, int, int);
 template cudaError_t launch_step_tma<float>(const Geom &, const Coef<float> &, const CUtensorMap *, Fields<float>,
-                                            bool, bool, double *, int, int, int *, unsigned long long, int,
+                                            bool, bool, double *, const StepTune &, int *, unsigned long long, int,
                                             cudaStream_t);
 template cudaError_t launch_step_tma<double>(const Geom &, const Coef<double> &, const CUtensorMap *,
-                                             Fields<double>, bool, bool, double *, int, int, int *, unsigned long long,
-                                             int, cudaStream_t);
+                                             Fields<double>, bool, bool, double *, const StepTune &, int *,
+                                             unsigned long long, int, cudaStream_t);
 
 }  // namespace ppf

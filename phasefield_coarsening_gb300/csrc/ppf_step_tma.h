@@ -8,6 +8,13 @@
 
 namespace ppf {
 
+// Launch choices of the fused step that the autotuner may change.
+struct StepTune {
+    int grid;   // persistent CTAs
+    int zc;     // z planes per work item
+    int roll;   // 3: plane body unrolled three times; 1: one copy
+};
+
 // Tensor map of one padded field (3-D: x pitch, ny+2 rows, nz+2 planes)
 // with the kernel's box; 0 on success.
 template <typename T>
@@ -18,6 +25,10 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map);
 template <typename T>
 int tma_grid(const Geom &g, int num_sms, int *zc);
 
+// Grid for a given z chunk length.
+template <typename T>
+int tma_grid_for_zc(const Geom &g, int num_sms, int zc);
+
 // One fused step.  maps = {etaS, etaL, c} of the input state; eqA selects
 // the specialisation for AS == AL (mu needs no reciprocal); `partials`
 // (nullable) receives 3 doubles per CTA; `err` is a device word that a
@@ -25,7 +36,7 @@ int tma_grid(const Geom &g, int num_sms, int *zc);
 // test hook that makes one wait per CTA run out.
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
-                            bool eqA, double *partials, int grid, int zc, int *err, unsigned long long limit_ns,
+                            bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
                             int inject_stall, cudaStream_t s);
 
 }  // namespace ppf

@@ -235,3 +235,43 @@ def test_ppf_program_matches_reference_run(name, tmp_path):
     # identical text up to the last printed digit (sums agree to ~1e-14)
     for a, b in zip(my_lines, ref_lines):
         assert a.split("\t")[0].split(":")[0] == b.split("\t")[0].split(":")[0]
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_launch_choices_are_bit_identical(precision):
+    """The z chunk and the unroll change only who computes a cell, never the
+    arithmetic: every launch choice gives the same bits."""
+    shape = (40, 35, 70)
+    st = smooth_state(shape, seed=12)
+    ref = None
+    for zc, roll in [(None, None), (1, 3), (7, 1), (40, 3), (13, 1)]:
+        with ppf.Simulation(shape, bc=1, precision=precision) as s:
+            if zc is not None:
+                s.set_tune(zc, roll)
+            s.upload(*st)
+            s.step(6)
+            out = s.download()
+        if ref is None:
+            ref = out
+        else:
+            for a, b in zip(out, ref):
+                assert np.array_equal(a, b), (zc, roll)
+
+
+def test_autotune_keeps_state_and_picks_a_valid_choice():
+    shape = (64, 48, 130)
+    st = smooth_state(shape, seed=13)
+    with ppf.Simulation(shape, precision="f32") as s:
+        s.upload(*st)
+        s.step(3)
+        before = s.download()
+        t = s.autotune(trial_steps=3)
+        after = s.download()
+        assert t["roll"] in (1, 3) and 1 <= t["zc"] <= shape[0] and t["us_per_step"] > 0
+        assert s.get_tune()["zc"] == t["zc"] and s.reduce()["steps"] == 3
+        for a, b in zip(before, after):
+            assert np.array_equal(a, b)
+        s.step(4)
+        got = s.download()
+    ref = oracle.run(*st, 7, bc=0)
+    assert max(float(np.abs(a - b).max()) for a, b in zip(got, ref[:3])) <= 1e-5

@@ -63,6 +63,7 @@ struct alignas(128) TmaSmem {
     using G = TmaGeo<T>;
     T raw[G::S][3][G::BOX_PAD];   // etaS, etaL, c boxes per stage
     T mm[3][2][G::BOX];           // mu, M of three consecutive planes
+    T gstage[G::NT][G::CY][3];    // new values of a thread's boundary cells, for their ghosts
     unsigned long long bar[G::S];
     int abort;
 };
@@ -343,6 +344,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     const T *nS = sm.raw[st_prev][0], *nL = sm.raw[st_prev][1];
                     const T *nmu = sm.mm[mb_prev][0], *nM = sm.mm[mb_prev][1];
                     const bool zface = q == 0 || q == g.nz - 1;
+                    const unsigned gm = vmask & (zface ? ~0u : emask);   // own cells that feed ghosts
                     const int64_t base = col + (int64_t)(q + 1) * g.PS;
 #pragma unroll
                     for (int j = 0; j < CY; ++j) {
@@ -365,6 +367,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                         const int64_t a = base + (int64_t)j * g.P;
                         if (C_ONLY) {
                             out.c[a] = cn;
+                            if (gm & (1u << j)) sm.gstage[tid][j][2] = cn;
                             if (STATS) acc[0] += (double)fl * (double)fl;
                         } else {
                             const T eS = Qr.S[j], eL = Qr.L[j], dmu = Qr.d[j];
@@ -380,6 +383,11 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             out.eS[a] = eS + dS;
                             out.eL[a] = eL + dL;
                             out.c[a] = cn;
+                            if (gm & (1u << j)) {
+                                sm.gstage[tid][j][0] = eS + dS;
+                                sm.gstage[tid][j][1] = eL + dL;
+                                sm.gstage[tid][j][2] = cn;
+                            }
                             if (STATS) {
                                 acc[0] += (double)fl * (double)fl;
                                 acc[1] += (double)dS * (double)dS;
@@ -387,18 +395,16 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             }
                         }
                     }
-                    // face ghosts of this thread's boundary cells: read back the
-                    // values it just stored (own writes, program order) and copy
-                    // them to the ghosts; one compact loop instead of a copy per cell
-                    const unsigned gm = vmask & (zface ? ~0u : emask);
+                    // face ghosts of this thread's boundary cells, from the values
+                    // staged in shared memory above: one compact loop instead of a
+                    // copy of the ghost code per cell
                     if (gm) {
 #pragma unroll 1
                         for (int j = 0; j < CY; ++j) {
                             if (!(gm & (1u << j))) continue;
                             const int64_t a = base + (int64_t)j * g.P;
-                            const T c = out.c[a];
-                            const T sv = C_ONLY ? T(0) : out.eS[a], lv = C_ONLY ? T(0) : out.eL[a];
-                            store_ghosts<T, C_ONLY>(g, out, a, X, y0 + ty0 + j, q, sv, lv, c);
+                            store_ghosts<T, C_ONLY>(g, out, a, X, y0 + ty0 + j, q, sm.gstage[tid][j][0],
+                                                    sm.gstage[tid][j][1], sm.gstage[tid][j][2]);
                         }
                     }
                 }

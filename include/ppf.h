@@ -181,6 +181,28 @@ int ppf_set_tune(ppf_ctx *ctx, const ppf_tune *t);
  * choice and its time per step. */
 int ppf_autotune(ppf_ctx *ctx, int trial_steps, ppf_tune *best);
 
+/* Allocation-free observables.  No counterpart in the reference.
+ *
+ * For callers that may not allocate device memory: typically a hook that a
+ * host application calls between its own steps, whose device memory belongs
+ * to the application's pool or arena (a caching allocator, preallocated
+ * communication buffers), where an unplanned cudaMalloc can fail on a full
+ * device, fragment the pool, or hold up the application's streams.  The
+ * caller passes its own device arrays -- etaS, etaL, c, each nz*ny*nx
+ * doubles in C order [z][y][x] -- and a device array `out` of 5 doubles; the
+ * call queues the reduction on `stream` (NULL: the default stream) and
+ * returns.  out = {mass, solid, solid_cells, free_energy, nonfinite}, the
+ * same quantities as the matching fields of ppf_reduce.  Nothing is
+ * allocated: the partial sums go to a fixed device array of the library,
+ * which limits a call to PPF_NOALLOC_MAX_CELLS cells (larger grids get
+ * PPF_EINVAL with a message).  The first call on a device looks up that
+ * array's device address (do it before any stream capture).  Every call
+ * shares the array: calls that overlap on the GPU race, so issue them on
+ * one stream. */
+#define PPF_NOALLOC_MAX_CELLS 134217728   /* 512^3 */
+int ppf_observe_noalloc(int nz, int ny, int nx, const ppf_params *p, int bc, const double *etaS,
+                        const double *etaL, const double *c, double *out, void *stream);
+
 /* Message for the calling thread's last failure ("" if none). */
 const char *ppf_last_error(void);
 

@@ -28,7 +28,7 @@ EXPORTS = (
     "ppf_params_default", "ppf_params_derive", "ppf_create", "ppf_destroy", "ppf_get_dims", "ppf_set_stream",
     "ppf_upload", "ppf_download", "ppf_upload_device", "ppf_download_device", "ppf_step", "ppf_step_c_only",
     "ppf_reduce", "ppf_sync", "ppf_set_wait_limit", "ppf_debug_inject", "ppf_get_tune", "ppf_set_tune",
-    "ppf_autotune", "ppf_last_error", "ppf_version",
+    "ppf_autotune", "ppf_observe_noalloc", "ppf_last_error", "ppf_version",
     "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_last_error",
 )
 

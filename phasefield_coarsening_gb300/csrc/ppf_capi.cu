@@ -31,6 +31,8 @@ static int seterr(int code, const char *fmt, ...) {
     return code;
 }
 
+int ppf::set_last_error(int code, const char *msg) { return seterr(code, "%s", msg); }
+
 #define CU(call)                                                                                      \
     do {                                                                                              \
         cudaError_t e_ = (call);                                                                      \

@@ -78,6 +78,9 @@ template <typename T>
 cudaError_t launch_observe(const Geom &g, const CoefD &k, Fields<const T> f, double *partials,
                            int nblocks, cudaStream_t s);
 
+// Record `msg` as the calling thread's ppf_last_error() text; returns code.
+int set_last_error(int code, const char *msg);
+
 // Deterministic final sum: out[i] = sum_b partials[stride*b + i] for
 // i < nvals (fixed order, one CTA).
 cudaError_t launch_final_sum(const double *partials, int nblocks, int stride, int nvals, double *out,

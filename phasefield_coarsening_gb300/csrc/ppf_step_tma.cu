@@ -8,22 +8,19 @@
 // Data flow of one CTA:
 //   * (z chunk, x-y tile) work items in chunk-major order, dealt round-robin
 //     to a persistent grid; each item is a tile column segment marched up z;
-//   * every plane's etaS/etaL/c tile plus a one-cell ring (a TX+2*XH by
-//     TY+2 box per field) is streamed from HBM into an S-stage shared ring
-//     with cp.async.bulk.tensor.3d, completion signalled on the stage's
-//     mbarrier; S-1 planes are in flight while one is computed;
+//   * thread 0 streams every plane's etaS/etaL/c tile plus a one-cell ring
+//     (a TX+2*XH by TY+2 box per field) from HBM into a S-stage shared ring
+//     with cp.async.bulk.tensor.3d, completion signalled on an mbarrier per
+//     stage; S-2 planes are in flight while one is computed;
 //   * pass A (hS, mu, M) is evaluated once per loaded cell into a 3-plane
 //     shared ring of mu/M; each thread owns CY cells stacked in y so that
 //     its y and z neighbours stay in registers;
 //   * pass B + C for plane z-1 then read x/y neighbours from shared memory,
 //     and write the new state straight to HBM, including the face ghosts
 //     the boundary condition defines (so the next step reads ready ghosts).
-// There is no CTA-wide barrier per plane: the mu/M ring has a full and an
-// empty mbarrier per buffer, and a raw stage is refilled by whichever warp
-// releases it last, so warps drift up to a plane apart.  Every mbarrier
-// wait is bounded by a time limit: on expiry the warp stops, the CTA sets
-// an error word, drains its own outstanding copies (again bounded) and
-// exits; the host reports PPF_ETIMEOUT.
+// Every mbarrier wait is bounded by a time limit: on expiry the CTA sets an
+// error word, drains its own outstanding copies (again bounded) and exits
+// uniformly; the host reports PPF_ETIMEOUT.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
@@ -67,11 +64,7 @@ struct alignas(128) TmaSmem {
     T raw[G::S][3][G::BOX_PAD];   // etaS, etaL, c boxes per stage
     T mm[3][2][G::BOX];           // mu, M of three consecutive planes
     T gstage[G::NT][G::CY][3];    // new values of a thread's boundary cells, for their ghosts
-    unsigned long long full[G::S];    // raw stage s holds its load (TMA complete_tx)
-    unsigned long long mfull[3];      // mu/M plane buffer b written by every thread
-    unsigned long long mempty[3];     // mu/M plane buffer b read by every thread
-    int released[G::S];               // warps done with raw stage s (the last one refills it)
-    int last_issued[G::S];            // newest load index issued into stage s
+    unsigned long long bar[G::S];
     int abort;
 };
 
@@ -96,10 +89,6 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
@@ -222,25 +211,6 @@ struct ItemWalk {
 };
 
 // Registers of the own cells of one plane.
-// Random access into a CTA's load sequence: load k -> (tile, plane).
-struct LoadMap {
-    int first, stride, nitems, ntiles, zc, nz;
-    __device__ __forceinline__ bool at(int k, int &tile, int &pz) const {
-        for (int item = first; item < nitems; item += stride) {
-            const int c = item / ntiles;
-            const int z0 = c * zc, z1 = min(nz, z0 + zc);
-            const int n = z1 - z0 + 2;
-            if (k < n) {
-                tile = item - c * ntiles;
-                pz = z0 - 1 + k;
-                return true;
-            }
-            k -= n;
-        }
-        return false;
-    }
-};
-
 template <typename T, int CY>
 struct PlaneRegs {
     T S[CY], L[CY], mu[CY], M[CY], c[CY], d[CY];
@@ -269,48 +239,37 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const int ob = (ty0 + 1) * BX + tx + XH;          // shared offset of the first own cell
 
     double acc[3] = {0.0, 0.0, 0.0};
-    constexpr int NW = G::NT / 32;
     if ((int)blockIdx.x < nitems) {
         if (tid == 0) {
-            for (int q = 0; q < S; ++q) {
-                mbar_init(smem_u32(&sm.full[q]), 1);
-                sm.released[q] = 0;
-                sm.last_issued[q] = -1;
-            }
-            for (int q = 0; q < 3; ++q) {
-                mbar_init(smem_u32(&sm.mfull[q]), G::NT);
-                mbar_init(smem_u32(&sm.mempty[q]), G::NT);
-            }
+            for (int s = 0; s < S; ++s) mbar_init(smem_u32(&sm.bar[s]), 1);
             sm.abort = 0;
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
         __syncthreads();
 
-        const LoadMap lmap{(int)blockIdx.x, (int)gridDim.x, nitems, ntiles, zc, g.nz};
-        // issue load k into its stage (any thread; the stage must be free)
-        auto issue = [&](int k) {
-            int tile, pz;
-            if (!lmap.at(k, tile, pz)) return;
-            const int q = k % S;
-            const uint32_t bar = smem_u32(&sm.full[q]);
-            const int bx = tile % ntx, by = tile / ntx;
+        // producer (thread 0): next load to issue, its stage, loads issued
+        ItemWalk prod;
+        prod.start(blockIdx.x, gridDim.x, nitems, ntiles, zc, g.nz);
+        int ist = 0, issued = 0;
+        auto issue = [&]() {
+            const uint32_t bar = smem_u32(&sm.bar[ist]);
+            const int bx = prod.tile % ntx, by = prod.tile / ntx;
             const int xs = bx * TX + g.xoff - XH;     // storage x of the box start (16-byte aligned)
             const int ys = by * TY;                    // storage y of interior y0-1
-            const int zs = pz + 1;                     // storage z of the plane
+            const int zs = prod.pz + 1;                // storage z of the plane
             uint32_t bytes = 3u * (uint32_t)G::BOX_BYTES;
-            if (inject_stall && k == 1) bytes += 16u;  // test hook: this phase can never complete
-            sm.last_issued[q] = k;
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            if (inject_stall && issued == 1) bytes += 16u;   // test hook: this phase can never complete
             mbar_expect_tx(bar, bytes);
-            tma_load_3d(smem_u32(sm.raw[q][0]), &mapS, xs, ys, zs, bar);
-            tma_load_3d(smem_u32(sm.raw[q][1]), &mapL, xs, ys, zs, bar);
-            tma_load_3d(smem_u32(sm.raw[q][2]), &mapC, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][0]), &mapS, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][1]), &mapL, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][2]), &mapC, xs, ys, zs, bar);
+            prod.advance();
+            ist = ist + 1 == S ? 0 : ist + 1;
+            ++issued;
         };
-        // every stage starts filled: the refill after load l-1 is released
-        // issues load l-1+S into that same stage
         if (tid == 0)
-            for (int k = 0; k < S; ++k) issue(k);
+            for (int l = 0; l < S - 2 && prod.valid(); ++l) issue();
 
         // three register planes whose roles rotate: q-1, q, q+1
         PlaneRegs<T, CY> RA, RB, RC;
@@ -322,22 +281,10 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
 
         ItemWalk cons;
         cons.start(blockIdx.x, gridDim.x, nitems, ntiles, zc, g.nz);
-        int l = 0;                                   // load being consumed
-        int st = 0, mb = 0, st_prev = 0, mb_prev = 0;
-        uint32_t par = 0;                            // phase parity of full[st]
+        int st = 0, mb = 0, consumed = 0;            // stage / mu-M buffer / count of the current load
+        uint32_t par = 0;
+        int st_prev = 0, mb_prev = 0;
         bool dead = false;
-        // bounded wait; a timeout in any lane stops the whole warp (the vote
-        // keeps `dead` warp-uniform, so no lane is left alone in __syncwarp)
-        auto bounded = [&](uint32_t bar, uint32_t parity) {
-            const bool timed_out = !mbar_wait(bar, parity, limit_ns);
-            if (__any_sync(0xffffffffu, timed_out)) {
-                if (lane == 0) {
-                    sm.abort = 1;
-                    atomicOr(err, 1);
-                }
-                dead = true;
-            }
-        };
         while (cons.valid() && !dead) {
             const int bx = cons.tile % ntx, by = cons.tile / ntx;
             const int x0 = bx * TX, y0 = by * TY, z0 = cons.z0, z1 = cons.z1;
@@ -352,14 +299,14 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             }
             const int64_t col = (int64_t)(y0 + ty0 + 1) * g.P + X + g.xoff;   // storage of own cell j=0, z=-1
 
-            // one plane: pass A of load l (plane pz) into Xr, then pass B + C of
-            // load l-1 (plane pz-1) from (Pr = pz-2, Qr = pz-1, Xr = pz), then
-            // the releases of load l-1; false once the item is done
+            // one plane: load/pass A of plane pz into Xr, pass B + C of plane pz-1
+            // from (Pr = pz-2, Qr = pz-1, Xr = pz); false once the item is done
             auto plane = [&](int pz, PlaneRegs<T, CY> &Pr, PlaneRegs<T, CY> &Qr, PlaneRegs<T, CY> &Xr) -> bool {
-                if (pz > z1 || dead) return false;
-                bounded(smem_u32(&sm.full[st]), par);                                  // raw data of load l
-                if (l >= 3) bounded(smem_u32(&sm.mempty[mb]), (uint32_t)(((l / 3) - 1) & 1));   // buffer free
-                if (dead) return false;
+                if (pz > z1) return false;
+                if (!mbar_wait(smem_u32(&sm.bar[st]), par, limit_ns)) {
+                    sm.abort = 1;
+                    atomicOr(err, 1);
+                }
                 const T *rS = sm.raw[st][0], *rL = sm.raw[st][1], *rC = sm.raw[st][2];
                 T *wmu = sm.mm[mb][0], *wM = sm.mm[mb][1];
 #pragma unroll
@@ -388,12 +335,12 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     wmu[o] = mu;
                     wM[o] = M;
                 }
-                mbar_arrive(smem_u32(&sm.mfull[mb]));
+                __syncthreads();
+                if (sm.abort) { dead = true; return false; }
+                if (tid == 0 && prod.valid()) issue();   // refill the stage freed two planes ago
 
                 const int q = pz - 1;
                 if (q >= z0) {
-                    bounded(smem_u32(&sm.mfull[mb_prev]), (uint32_t)(((l - 1) / 3) & 1));   // neighbours' pass A
-                    if (dead) return false;
                     const T *nS = sm.raw[st_prev][0], *nL = sm.raw[st_prev][1];
                     const T *nmu = sm.mm[mb_prev][0], *nM = sm.mm[mb_prev][1];
                     const bool zface = q == 0 || q == g.nz - 1;
@@ -461,21 +408,11 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                         }
                     }
                 }
-                if (l >= 1) {
-                    // load l-1 is done with: its mu/M buffer, and its raw stage --
-                    // the last warp to let go of the stage refills it, S-1 loads ahead
-                    mbar_arrive(smem_u32(&sm.mempty[mb_prev]));
-                    __syncwarp();
-                    if (lane == 0 && atomicAdd(&sm.released[st_prev], 1) == NW - 1) {
-                        sm.released[st_prev] = 0;
-                        issue(l - 1 + S);
-                    }
-                }
                 st_prev = st;
                 mb_prev = mb;
                 if (++st == S) { st = 0; par ^= 1u; }
                 mb = mb + 1 == 3 ? 0 : mb + 1;
-                ++l;
+                ++consumed;
                 return true;
             };
             if (ROLL == 3) {
@@ -497,15 +434,11 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             }
             if (!dead) cons.next_item();
         }
-        // every wait above is bounded, so every thread gets here
-        __syncthreads();
-        if (sm.abort) {
-            // a wait ran out: drain the copies still in flight (bounded), then leave
+        if (dead) {
+            // drain this CTA's own copies still in flight (bounded), then leave
             if (tid == 0)
-                for (int q = 0; q < S; ++q) {
-                    const int k = sm.last_issued[q];
-                    if (k >= 0) (void)mbar_wait(smem_u32(&sm.full[q]), (uint32_t)((k / S) & 1), limit_ns);
-                }
+                for (int d = 0; d < issued - consumed; ++d)
+                    (void)mbar_wait(smem_u32(&sm.bar[(st + d) % S]), par ^ (uint32_t)(((st + d) / S) & 1), limit_ns);
             return;
         }
     }

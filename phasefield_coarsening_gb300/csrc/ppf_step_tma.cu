@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 #include "ppf_internal.h"
 #include "ppf_step_tma.h"
@@ -158,6 +159,93 @@ __device__ __forceinline__ void pass_a_own(const Coef<T> &k, T eS, T eL, T c, T 
     dmu = k.dm2 * (eS * eL) * (rs * rs) * D;
 }
 
+// Two cells of one thread evaluated together.  For float this is the
+// packed f32x2 arithmetic of sm_100+ (one instruction per pair); for double
+// it is plain scalar code.  Each lane is rounded exactly as the scalar
+// operation would be.
+template <typename T>
+struct V2;
+
+template <>
+struct V2<float> {
+    float2 v;
+    __device__ __forceinline__ V2() {}
+    __device__ __forceinline__ V2(float a, float b) : v(make_float2(a, b)) {}
+    __device__ __forceinline__ explicit V2(float2 w) : v(w) {}
+    __device__ __forceinline__ float x() const { return v.x; }
+    __device__ __forceinline__ float y() const { return v.y; }
+};
+__device__ __forceinline__ V2<float> operator+(V2<float> a, V2<float> b) { return V2<float>(__fadd2_rn(a.v, b.v)); }
+__device__ __forceinline__ V2<float> operator*(V2<float> a, V2<float> b) { return V2<float>(__fmul2_rn(a.v, b.v)); }
+__device__ __forceinline__ V2<float> operator-(V2<float> a, V2<float> b) {
+    unsigned long long ra, xa, ya;
+    memcpy(&xa, &a.v, 8);
+    memcpy(&ya, &b.v, 8);
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(ra) : "l"(xa), "l"(ya));
+    float2 r;
+    memcpy(&r, &ra, 8);
+    return V2<float>(r);
+}
+__device__ __forceinline__ V2<float> fma2(V2<float> a, V2<float> b, V2<float> c) {
+    return V2<float>(__ffma2_rn(a.v, b.v, c.v));
+}
+
+template <>
+struct V2<double> {
+    double a, b;
+    __device__ __forceinline__ V2() {}
+    __device__ __forceinline__ V2(double p, double q) : a(p), b(q) {}
+    __device__ __forceinline__ double x() const { return a; }
+    __device__ __forceinline__ double y() const { return b; }
+};
+__device__ __forceinline__ V2<double> operator+(V2<double> p, V2<double> q) { return V2<double>(p.a + q.a, p.b + q.b); }
+__device__ __forceinline__ V2<double> operator*(V2<double> p, V2<double> q) { return V2<double>(p.a * q.a, p.b * q.b); }
+__device__ __forceinline__ V2<double> operator-(V2<double> p, V2<double> q) { return V2<double>(p.a - q.a, p.b - q.b); }
+__device__ __forceinline__ V2<double> fma2(V2<double> p, V2<double> q, V2<double> r) {
+    return V2<double>(fma(p.a, q.a, r.a), fma(p.b, q.b, r.b));
+}
+
+template <typename T>
+__device__ __forceinline__ V2<T> splat(T a) { return V2<T>(a, a); }
+
+// pass A + the centre part of pass B (see pass_a_own) for a pair of cells
+template <typename T, bool EQ>
+__device__ __forceinline__ void pass_a_own2(const Coef<T> &k, V2<T> eS, V2<T> eL, V2<T> c, V2<T> &mu, V2<T> &Mt,
+                                            V2<T> &dmu) {
+    const V2<T> S2 = eS * eS;
+    const V2<T> s2 = fma2(eL, eL, S2);
+    const V2<T> rs(fast_rcp(s2.x()), fast_rcp(s2.y()));
+    const V2<T> h = S2 * rs;
+    const V2<T> w = fma2(h, splat(k.dc0), c - splat(k.cL0));
+    if (EQ) {
+        mu = splat(k.A) * w;
+    } else {
+        const V2<T> den = fma2(h, splat(k.dA), splat(k.AS));
+        mu = splat(k.AsAl) * V2<T>(fast_rcp(den.x()), fast_rcp(den.y())) * w;
+    }
+    Mt = fma2(h, splat(k.Mt1), splat(k.Mt0));
+    const V2<T> D = EQ ? fma2(mu, splat(-k.q1), splat(k.dC))
+                       : splat(k.dC) - mu * fma2(mu, splat(k.q2), splat(k.q1));
+    dmu = splat(k.dm2) * (eS * eL) * (rs * rs) * D;
+}
+
+// pass A alone for a pair (c-only steps)
+template <typename T, bool EQ>
+__device__ __forceinline__ void pass_a2(const Coef<T> &k, V2<T> eS, V2<T> eL, V2<T> c, V2<T> &mu, V2<T> &Mt) {
+    const V2<T> S2 = eS * eS;
+    const V2<T> s2 = fma2(eL, eL, S2);
+    const V2<T> rs(fast_rcp(s2.x()), fast_rcp(s2.y()));
+    const V2<T> h = S2 * rs;
+    const V2<T> w = fma2(h, splat(k.dc0), c - splat(k.cL0));
+    if (EQ) {
+        mu = splat(k.A) * w;
+    } else {
+        const V2<T> den = fma2(h, splat(k.dA), splat(k.AS));
+        mu = splat(k.AsAl) * V2<T>(fast_rcp(den.x()), fast_rcp(den.y())) * w;
+    }
+    Mt = fma2(h, splat(k.Mt1), splat(k.Mt0));
+}
+
 // Face ghosts fed by a boundary cell (the BC fill of phasefield.c:1112-1189
 // applied to the new state): along an axis of n cells and stride st, cell 0
 // is copied to ghost n (periodic) or -1 (no-flux), cell n-1 to ghost -1
@@ -210,10 +298,12 @@ struct ItemWalk {
     __device__ __forceinline__ void advance() { if (++pz > z1) next_item(); }
 };
 
-// Registers of the own cells of one plane.
-template <typename T, int CY>
+// Registers of the own cells of one plane, as pairs (cell i, cell i+H) of
+// the thread's column of CY = 2H cells: with that pairing the y neighbours
+// of pair i are mostly the pairs i-1 and i+1 themselves.
+template <typename T, int H>
 struct PlaneRegs {
-    T S[CY], L[CY], mu[CY], M[CY], c[CY], d[CY];
+    V2<T> S[H], L[H], mu[H], M[H], c[H], d[H];
 };
 
 template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL>
@@ -272,11 +362,13 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             for (int l = 0; l < S - 2 && prod.valid(); ++l) issue();
 
         // three register planes whose roles rotate: q-1, q, q+1
-        PlaneRegs<T, CY> RA, RB, RC;
+        constexpr int H = CY / 2;
+        static_assert(CY % 2 == 0, "cells are processed in pairs");
+        PlaneRegs<T, H> RA, RB, RC;
 #pragma unroll
-        for (int j = 0; j < CY; ++j) {
-            RA.S[j] = RA.L[j] = RA.mu[j] = RA.M[j] = RA.c[j] = RA.d[j] = T(0);
-            RB.S[j] = RB.L[j] = RB.mu[j] = RB.M[j] = RB.c[j] = RB.d[j] = T(0);
+        for (int i = 0; i < H; ++i) {
+            RA.S[i] = RA.L[i] = RA.mu[i] = RA.M[i] = RA.c[i] = RA.d[i] = splat(T(0));
+            RB.S[i] = RB.L[i] = RB.mu[i] = RB.M[i] = RB.c[i] = RB.d[i] = splat(T(0));
         }
 
         ItemWalk cons;
@@ -301,7 +393,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
 
             // one plane: load/pass A of plane pz into Xr, pass B + C of plane pz-1
             // from (Pr = pz-2, Qr = pz-1, Xr = pz); false once the item is done
-            auto plane = [&](int pz, PlaneRegs<T, CY> &Pr, PlaneRegs<T, CY> &Qr, PlaneRegs<T, CY> &Xr) -> bool {
+            auto plane = [&](int pz, PlaneRegs<T, H> &Pr, PlaneRegs<T, H> &Qr, PlaneRegs<T, H> &Xr) -> bool {
                 if (pz > z1) return false;
                 if (!mbar_wait(smem_u32(&sm.bar[st]), par, limit_ns)) {
                     sm.abort = 1;
@@ -310,18 +402,20 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 const T *rS = sm.raw[st][0], *rL = sm.raw[st][1], *rC = sm.raw[st][2];
                 T *wmu = sm.mm[mb][0], *wM = sm.mm[mb][1];
 #pragma unroll
-                for (int j = 0; j < CY; ++j) {
-                    const int o = ob + j * BX;
-                    Xr.S[j] = rS[o];
-                    Xr.L[j] = rL[o];
-                    Xr.c[j] = rC[o];
+                for (int i = 0; i < H; ++i) {
+                    const int o0 = ob + i * BX, o1 = o0 + H * BX;     // cells i and i+H
+                    Xr.S[i] = V2<T>(rS[o0], rS[o1]);
+                    Xr.L[i] = V2<T>(rL[o0], rL[o1]);
+                    Xr.c[i] = V2<T>(rC[o0], rC[o1]);
                     if (C_ONLY) {
-                        (void)pass_a<T, EQ>(k, Xr.S[j], Xr.L[j], Xr.c[j], Xr.mu[j], Xr.M[j]);
+                        pass_a2<T, EQ>(k, Xr.S[i], Xr.L[i], Xr.c[i], Xr.mu[i], Xr.M[i]);
                     } else {
-                        pass_a_own<T, EQ>(k, Xr.S[j], Xr.L[j], Xr.c[j], Xr.mu[j], Xr.M[j], Xr.d[j]);
+                        pass_a_own2<T, EQ>(k, Xr.S[i], Xr.L[i], Xr.c[i], Xr.mu[i], Xr.M[i], Xr.d[i]);
                     }
-                    wmu[o] = Xr.mu[j];
-                    wM[o] = Xr.M[j];
+                    wmu[o0] = Xr.mu[i].x();
+                    wmu[o1] = Xr.mu[i].y();
+                    wM[o0] = Xr.M[i].x();
+                    wM[o1] = Xr.M[i].y();
                 }
                 if (tid < G::RING) {                   // the one-cell ring around the tile
                     int hx, hy;
@@ -347,51 +441,88 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     const unsigned gm = vmask & (zface ? ~0u : emask);   // own cells that feed ghosts
                     const int64_t base = col + (int64_t)(q + 1) * g.PS;
 #pragma unroll
-                    for (int j = 0; j < CY; ++j) {
-                        if (!(vmask & (1u << j))) continue;
-                        const int o = ob + j * BX;
-                        const T mu = Qr.mu[j], M = Qr.M[j], c = Qr.c[j];
-                        const T muym = j > 0 ? Qr.mu[j - 1] : nmu[o - BX], Mym = j > 0 ? Qr.M[j - 1] : nM[o - BX];
-                        const T muyp = j < CY - 1 ? Qr.mu[j + 1] : nmu[o + BX];
-                        const T Myp = j < CY - 1 ? Qr.M[j + 1] : nM[o + BX];
+                    for (int i = 0; i < H; ++i) {
+                        const int j0 = i, j1 = i + H;                       // the pair's cells
+                        const bool v0 = vmask & (1u << j0), v1 = vmask & (1u << j1);
+                        if (!(v0 || v1)) continue;
+                        const int o0 = ob + j0 * BX, o1 = ob + j1 * BX;
+                        const V2<T> mu = Qr.mu[i], M = Qr.M[i], c = Qr.c[i];
+                        // y neighbours: pair i-1 / i+1, or a shared row at the column ends
+                        const V2<T> muym = i > 0 ? Qr.mu[i - 1] : V2<T>(nmu[o0 - BX], Qr.mu[H - 1].x());
+                        const V2<T> Mym = i > 0 ? Qr.M[i - 1] : V2<T>(nM[o0 - BX], Qr.M[H - 1].x());
+                        const V2<T> muyp = i < H - 1 ? Qr.mu[i + 1] : V2<T>(Qr.mu[0].y(), nmu[o1 + BX]);
+                        const V2<T> Myp = i < H - 1 ? Qr.M[i + 1] : V2<T>(Qr.M[0].y(), nM[o1 + BX]);
+                        const V2<T> muxp(nmu[o0 + 1], nmu[o1 + 1]), muxm(nmu[o0 - 1], nmu[o1 - 1]);
+                        const V2<T> Mxp(nM[o0 + 1], nM[o1 + 1]), Mxm(nM[o0 - 1], nM[o1 - 1]);
                         // dc: the flux form of phasefield.c:374-384, tmp3 inside M'.
                         // The six face fluxes are summed first and added to c once,
                         // so c is rounded once per step.
-                        T fl = (Xr.M[j] + M) * (Xr.mu[j] - mu);
-                        fl += (Pr.M[j] + M) * (Pr.mu[j] - mu);
-                        fl += (Myp + M) * (muyp - mu);
-                        fl += (Mym + M) * (muym - mu);
-                        fl += (nM[o + 1] + M) * (nmu[o + 1] - mu);
-                        fl += (nM[o - 1] + M) * (nmu[o - 1] - mu);
-                        const T cn = c + fl;
-                        const int64_t a = base + (int64_t)j * g.P;
+                        V2<T> fl = (Xr.M[i] + M) * (Xr.mu[i] - mu);
+                        fl = fma2(Pr.M[i] + M, Pr.mu[i] - mu, fl);
+                        fl = fma2(Myp + M, muyp - mu, fl);
+                        fl = fma2(Mym + M, muym - mu, fl);
+                        fl = fma2(Mxp + M, muxp - mu, fl);
+                        fl = fma2(Mxm + M, muxm - mu, fl);
+                        const V2<T> cn = c + fl;
+                        const int64_t a0 = base + (int64_t)j0 * g.P, a1 = base + (int64_t)j1 * g.P;
                         if (C_ONLY) {
-                            out.c[a] = cn;
-                            if (gm & (1u << j)) sm.gstage[tid][j][2] = cn;
-                            if (STATS) acc[0] += (double)fl * (double)fl;
+                            if (v0) out.c[a0] = cn.x();
+                            if (v1) out.c[a1] = cn.y();
+                            if (gm & (1u << j0)) sm.gstage[tid][j0][2] = cn.x();
+                            if (gm & (1u << j1)) sm.gstage[tid][j1][2] = cn.y();
+                            if (STATS) {
+                                if (v0) acc[0] += (double)fl.x() * (double)fl.x();
+                                if (v1) acc[0] += (double)fl.y() * (double)fl.y();
+                            }
                         } else {
-                            const T eS = Qr.S[j], eL = Qr.L[j], dmu = Qr.d[j];
-                            const T Sym = j > 0 ? Qr.S[j - 1] : nS[o - BX], Syp = j < CY - 1 ? Qr.S[j + 1] : nS[o + BX];
-                            const T Lym = j > 0 ? Qr.L[j - 1] : nL[o - BX], Lyp = j < CY - 1 ? Qr.L[j + 1] : nL[o + BX];
+                            const V2<T> eS = Qr.S[i], eL = Qr.L[i], dmu = Qr.d[i];
+                            const V2<T> Sym = i > 0 ? Qr.S[i - 1] : V2<T>(nS[o0 - BX], Qr.S[H - 1].x());
+                            const V2<T> Lym = i > 0 ? Qr.L[i - 1] : V2<T>(nL[o0 - BX], Qr.L[H - 1].x());
+                            const V2<T> Syp = i < H - 1 ? Qr.S[i + 1] : V2<T>(Qr.S[0].y(), nS[o1 + BX]);
+                            const V2<T> Lyp = i < H - 1 ? Qr.L[i + 1] : V2<T>(Qr.L[0].y(), nL[o1 + BX]);
                             // detaS, detaL of phasefield.c:360-373 with tmp1 absorbed:
                             //   eta (mt eta^2 + g2 other^2 + e0) - kt sum6 -/+ other tmp1 dmu
-                            const T S6 = Xr.S[j] + Pr.S[j] + Syp + Sym + nS[o + 1] + nS[o - 1];
-                            const T L6 = Xr.L[j] + Pr.L[j] + Lyp + Lym + nL[o + 1] + nL[o - 1];
-                            const T S2 = eS * eS, L2 = eL * eL;
-                            const T dS = eS * (k.mt * S2 + (k.g2 * L2 + k.e0)) - k.kt * S6 + eL * dmu;
-                            const T dL = eL * (k.mt * L2 + (k.g2 * S2 + k.e0)) - k.kt * L6 - eS * dmu;
-                            out.eS[a] = eS + dS;
-                            out.eL[a] = eL + dL;
-                            out.c[a] = cn;
-                            if (gm & (1u << j)) {
-                                sm.gstage[tid][j][0] = eS + dS;
-                                sm.gstage[tid][j][1] = eL + dL;
-                                sm.gstage[tid][j][2] = cn;
+                            const V2<T> S6 = Xr.S[i] + Pr.S[i] + Syp + Sym + V2<T>(nS[o0 + 1], nS[o1 + 1]) +
+                                             V2<T>(nS[o0 - 1], nS[o1 - 1]);
+                            const V2<T> L6 = Xr.L[i] + Pr.L[i] + Lyp + Lym + V2<T>(nL[o0 + 1], nL[o1 + 1]) +
+                                             V2<T>(nL[o0 - 1], nL[o1 - 1]);
+                            const V2<T> S2 = eS * eS, L2 = eL * eL;
+                            const V2<T> nkt = splat(-k.kt);
+                            const V2<T> dS = fma2(eL, dmu, fma2(S6, nkt, eS * fma2(S2, splat(k.mt), fma2(L2, splat(k.g2), splat(k.e0)))));
+                            const V2<T> ndmu = splat(T(0)) - dmu;
+                            const V2<T> dL = fma2(eS, ndmu, fma2(L6, nkt, eL * fma2(L2, splat(k.mt), fma2(S2, splat(k.g2), splat(k.e0)))));
+                            const V2<T> Sn = eS + dS, Ln = eL + dL;
+                            if (v0) {
+                                out.eS[a0] = Sn.x();
+                                out.eL[a0] = Ln.x();
+                                out.c[a0] = cn.x();
+                            }
+                            if (v1) {
+                                out.eS[a1] = Sn.y();
+                                out.eL[a1] = Ln.y();
+                                out.c[a1] = cn.y();
+                            }
+                            if (gm & (1u << j0)) {
+                                sm.gstage[tid][j0][0] = Sn.x();
+                                sm.gstage[tid][j0][1] = Ln.x();
+                                sm.gstage[tid][j0][2] = cn.x();
+                            }
+                            if (gm & (1u << j1)) {
+                                sm.gstage[tid][j1][0] = Sn.y();
+                                sm.gstage[tid][j1][1] = Ln.y();
+                                sm.gstage[tid][j1][2] = cn.y();
                             }
                             if (STATS) {
-                                acc[0] += (double)fl * (double)fl;
-                                acc[1] += (double)dS * (double)dS;
-                                acc[2] += (double)dL * (double)dL;
+                                if (v0) {
+                                    acc[0] += (double)fl.x() * (double)fl.x();
+                                    acc[1] += (double)dS.x() * (double)dS.x();
+                                    acc[2] += (double)dL.x() * (double)dL.x();
+                                }
+                                if (v1) {
+                                    acc[0] += (double)fl.y() * (double)fl.y();
+                                    acc[1] += (double)dS.y() * (double)dS.y();
+                                    acc[2] += (double)dL.y() * (double)dL.y();
+                                }
                             }
                         }
                     }

@@ -125,8 +125,7 @@ static Coef<T> make_coef(const ppf_params &p, const ppf_derived &d) {
     k.q2 = (T)(0.5 * (1.0 / p.AS - 1.0 / p.AL));
     k.dm2 = (T)(2.0 * tmp1);
     k.mt = (T)(tmp1 * d.m);
-    k.g2 = (T)(2.0 * p.gamma * tmp1 * d.m);
-    k.e0 = (T)(6.0 * tmp1 * kh2 - tmp1 * d.m);
+    k.tg = (T)(2.0 * p.gamma);
     k.kt = (T)(tmp1 * kh2);
     return k;
 }

@@ -52,7 +52,7 @@ struct Coef {
     T Mt0, Mt1;       // tmp3*ML, tmp3*(MS-ML): M' = tmp3 M = Mt0 + Mt1 h
     T dC, q1, q2;     // CS-CL, cS0-cL0, (1/AS-1/AL)/2: driving force D = dC - mu (q1 + q2 mu)
     T dm2;            // 2 tmp1: tmp1 dmu = dm2 etaS etaL / (etaS^2+etaL^2)^2 D
-    T mt, g2, e0, kt; // tmp1 m, 2 gamma tmp1 m, 6 tmp1 kappa h2 - tmp1 m, tmp1 kappa h2
+    T mt, tg, kt;     // tmp1 m, 2 gamma, tmp1 kappa h2
 };
 
 // The same coefficients in double, plus what the observables need.

@@ -480,17 +480,19 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             const V2<T> Lym = i > 0 ? Qr.L[i - 1] : V2<T>(nL[o0 - BX], Qr.L[H - 1].x());
                             const V2<T> Syp = i < H - 1 ? Qr.S[i + 1] : V2<T>(Qr.S[0].y(), nS[o1 + BX]);
                             const V2<T> Lyp = i < H - 1 ? Qr.L[i + 1] : V2<T>(Qr.L[0].y(), nL[o1 + BX]);
-                            // detaS, detaL of phasefield.c:360-373 with tmp1 absorbed:
-                            //   eta (mt eta^2 + g2 other^2 + e0) - kt sum6 -/+ other tmp1 dmu
+                            // detaS, detaL of phasefield.c:360-373 with tmp1 absorbed, in
+                            // the reference's grouping  mt eta (eta^2 - 1 + 2 gamma other^2)
+                            //   - kt (sum6 - 6 eta) -/+ other tmp1 dmu,  which is exactly
+                            // zero for a pure phase (eta = 1, other = 0, flat neighbours)
                             const V2<T> S6 = Xr.S[i] + Pr.S[i] + Syp + Sym + V2<T>(nS[o0 + 1], nS[o1 + 1]) +
                                              V2<T>(nS[o0 - 1], nS[o1 - 1]);
                             const V2<T> L6 = Xr.L[i] + Pr.L[i] + Lyp + Lym + V2<T>(nL[o0 + 1], nL[o1 + 1]) +
                                              V2<T>(nL[o0 - 1], nL[o1 - 1]);
+                            const V2<T> one = splat(T(1)), tg = splat(k.tg), nkt = splat(-k.kt), m6 = splat(T(-6));
                             const V2<T> S2 = eS * eS, L2 = eL * eL;
-                            const V2<T> nkt = splat(-k.kt);
-                            const V2<T> dS = fma2(eL, dmu, fma2(S6, nkt, eS * fma2(S2, splat(k.mt), fma2(L2, splat(k.g2), splat(k.e0)))));
-                            const V2<T> ndmu = splat(T(0)) - dmu;
-                            const V2<T> dL = fma2(eS, ndmu, fma2(L6, nkt, eL * fma2(L2, splat(k.mt), fma2(S2, splat(k.g2), splat(k.e0)))));
+                            const V2<T> lapS = fma2(m6, eS, S6), lapL = fma2(m6, eL, L6);
+                            const V2<T> dS = fma2(splat(k.mt) * eS, fma2(tg, L2, S2 - one), fma2(nkt, lapS, eL * dmu));
+                            const V2<T> dL = fma2(splat(k.mt) * eL, fma2(tg, S2, L2 - one), fma2(nkt, lapL, splat(T(0)) - eS * dmu));
                             const V2<T> Sn = eS + dS, Ln = eL + dL;
                             if (v0) {
                                 out.eS[a0] = Sn.x();

@@ -162,6 +162,24 @@ int ppf_set_wait_limit(ppf_ctx *ctx, double seconds);
 #define PPF_INJECT_STALL_WAIT 1
 int ppf_debug_inject(ppf_ctx *ctx, int fault);
 
+/* Particle analysis of the current state (no counterpart in the
+ * reference, which leaves it to MATLAB post-processing, README.md:26).
+ * Particles are the 6-connected components of etaS > threshold, wrapping
+ * across periodic faces. */
+typedef struct ppf_particle_stats {
+    int64_t count;           /* number of particles */
+    double mean_radius;      /* R-bar: mean of (3V/4pi)^(1/3) over particles, in units of dx */
+    double solid_volume;     /* solid cells x dx^3 */
+    double largest_volume;   /* largest particle, cells x dx^3 */
+    double interface_area;   /* solid/liquid cell faces x dx^2 */
+} ppf_particle_stats;
+
+/* `volumes` (may be NULL) receives up to `capacity` particle volumes in
+ * cells, in no particular order; *nvolumes (may be NULL) the particle count.
+ * Device scratch of 8 bytes per cell is allocated on the first call. */
+int ppf_particles(ppf_ctx *ctx, double threshold, ppf_particle_stats *out, int64_t *volumes, int64_t capacity,
+                  int64_t *nvolumes);
+
 /* Launch choices of the fused step kernel.  No counterpart in the
  * reference (whose only tuning is the no-op cache blocking of
  * phasefield.c:58-62, :340-350). */

@@ -46,6 +46,8 @@ def lib():
         L.ppf_oracle_run.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64,
                                                           ctypes.c_int64] + [ctypes.c_void_p] * 4
         L.ppf_oracle_observe.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 4
+        L.ppf_oracle_particles.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
+                                                               ctypes.c_void_p, ctypes.c_int64]
         L.ppf_oracle_derive.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ppf_oracle_derive.restype = None
         _lib = L
@@ -89,3 +91,19 @@ def observe(etaS, etaL, c, bc=0, params=None) -> dict:
     if rc != 0:
         raise RuntimeError(f"oracle observe failed ({rc})")
     return {"mass": out[0], "solid": out[1], "solid_cells": out[2], "free_energy": out[3], "nonfinite": out[4]}
+
+
+def particles(etaS, bc=0, threshold=0.5) -> dict:
+    """Particles of etaS > threshold (6-connected, periodic wrap for bc=0)."""
+    a = np.ascontiguousarray(etaS, dtype=np.float64)
+    nz, ny, nx = a.shape
+    out = np.zeros(5)
+    cap = a.size
+    vols = np.zeros(cap, dtype=np.int64)
+    rc = lib().ppf_oracle_particles(nz, ny, nx, int(bc), a.ctypes.data, float(threshold), out.ctypes.data,
+                                    vols.ctypes.data, cap)
+    if rc != 0:
+        raise RuntimeError(f"oracle particles failed ({rc})")
+    n = int(out[0])
+    return {"count": n, "mean_radius": out[1] / n if n else 0.0, "solid_volume": out[2],
+            "largest_volume": out[3], "interface_area": out[4], "volumes": np.sort(vols[:n])}

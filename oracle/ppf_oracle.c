@@ -315,3 +315,73 @@ int ppf_oracle_observe(int nz, int ny, int nx, const ppf_params *p, int bc, cons
     out[0] = mass; out[1] = solid; out[2] = cnt; out[3] = F; out[4] = bad;
     return 0;
 }
+
+/* Particle analysis (no counterpart in the reference): 6-connected
+ * components of etaS > thr, wrapping across periodic faces.  out[0] count,
+ * out[1] sum of equivalent radii (3V/4pi)^(1/3) (cells, dx = 1), out[2]
+ * solid cells, out[3] largest particle (cells), out[4] solid/liquid faces.
+ * volumes (may be NULL) receives up to cap particle volumes, ordered by
+ * the smallest cell index of each particle. */
+static int64_t uf_find(int64_t *p, int64_t i)
+{
+    while (p[i] != i) {
+        p[i] = p[p[i]];
+        i = p[i];
+    }
+    return i;
+}
+
+int ppf_oracle_particles(int nz, int ny, int nx, int bc, const double *etaS, double thr, double out[5],
+                         int64_t *volumes, int64_t cap)
+{
+    if (nz < 1 || ny < 1 || nx < 1 || !etaS || !out) return -1;
+    const int64_t n = (int64_t)nz * ny * nx;
+    int64_t *p = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+    int64_t *v = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    if (!p || !v) { free(p); free(v); return -2; }
+    for (int64_t i = 0; i < n; ++i) p[i] = etaS[i] > thr ? i : -1;
+    double faces = 0;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const int64_t i = ((int64_t)z * ny + y) * nx + x;
+                const int c[3][3] = {{x + 1, y, z}, {x, y + 1, z}, {x, y, z + 1}};
+                const int lim[3] = {nx, ny, nz};
+                for (int d = 0; d < 3; ++d) {
+                    int q[3] = {c[d][0], c[d][1], c[d][2]};
+                    if (q[d] == lim[d]) {
+                        if (bc != PPF_BC_PERIODIC) continue;
+                        q[d] = 0;
+                    }
+                    const int64_t j = ((int64_t)q[2] * ny + q[1]) * nx + q[0];
+                    const int si = p[i] >= 0, sj = p[j] >= 0;
+                    if (si != sj) faces += 1.0;
+                    if (si && sj) {
+                        int64_t a = uf_find(p, i), b = uf_find(p, j);
+                        if (a != b) {
+                            if (a < b) p[b] = a;
+                            else p[a] = b;
+                        }
+                    }
+                }
+            }
+    double cnt = 0, rsum = 0, solid = 0, vmax = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (p[i] >= 0) {
+            v[uf_find(p, i)] += 1;
+            solid += 1;
+        }
+    int64_t k = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (p[i] == i) {
+            cnt += 1;
+            rsum += cbrt(3.0 * (double)v[i] / (4.0 * 3.14159265358979323846));
+            if ((double)v[i] > vmax) vmax = (double)v[i];
+            if (volumes && k < cap) volumes[k] = v[i];
+            ++k;
+        }
+    out[0] = cnt; out[1] = rsum; out[2] = solid; out[3] = vmax; out[4] = faces;
+    free(p);
+    free(v);
+    return 0;
+}

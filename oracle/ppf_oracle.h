@@ -29,6 +29,11 @@ int ppf_oracle_run(int nz, int ny, int nx, const ppf_params *p, int bc, int64_t 
 int ppf_oracle_observe(int nz, int ny, int nx, const ppf_params *p, int bc, const double *etaS,
                        const double *etaL, const double *c, double out[5]);
 
+/* particles of etaS > thr: count, sum of equivalent radii, solid cells,
+ * largest particle, solid/liquid faces; volumes by smallest cell index */
+int ppf_oracle_particles(int nz, int ny, int nx, int bc, const double *etaS, double thr, double out[5],
+                         int64_t *volumes, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,7 +28,7 @@ EXPORTS = (
     "ppf_params_default", "ppf_params_derive", "ppf_create", "ppf_destroy", "ppf_get_dims", "ppf_set_stream",
     "ppf_upload", "ppf_download", "ppf_upload_device", "ppf_download_device", "ppf_step", "ppf_step_c_only",
     "ppf_reduce", "ppf_sync", "ppf_set_wait_limit", "ppf_debug_inject", "ppf_get_tune", "ppf_set_tune",
-    "ppf_autotune", "ppf_observe_noalloc", "ppf_last_error", "ppf_version",
+    "ppf_autotune", "ppf_observe_noalloc", "ppf_particles", "ppf_last_error", "ppf_version",
     "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_last_error",
 )
 
@@ -63,6 +63,15 @@ class Stats(ctypes.Structure):
 class Tune(ctypes.Structure):
     """ppf_tune: launch choices of the fused step."""
     _fields_ = [("zc", ctypes.c_int), ("roll", ctypes.c_int), ("grid", ctypes.c_int), ("us_per_step", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class ParticleStats(ctypes.Structure):
+    """ppf_particle_stats."""
+    _fields_ = [("count", ctypes.c_int64), ("mean_radius", ctypes.c_double), ("solid_volume", ctypes.c_double),
+                ("largest_volume", ctypes.c_double), ("interface_area", ctypes.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -104,6 +113,8 @@ def lib() -> ctypes.CDLL:
         L.ppf_get_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
         L.ppf_set_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
         L.ppf_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Tune)]
+        L.ppf_particles.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ParticleStats),
+                                    ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
         L.ppf_get_dims.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 3
         L.ppf_h5_dims.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.ppf_h5_read3d.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _dp,
@@ -218,6 +229,22 @@ class Simulation:
     def set_tune(self, zc: int, roll: int = 3):
         t = Tune(int(zc), int(roll), 0, 0.0)
         _check(lib().ppf_set_tune(self._h, ctypes.byref(t)))
+
+    def particles(self, threshold: float = 0.5, volumes: bool = False) -> dict:
+        """Particles of etaS > threshold: count, mean radius R-bar, ...;
+        with volumes=True also the sorted particle volumes (cells)."""
+        st = ParticleStats()
+        n = ctypes.c_int64(0)
+        if volumes:
+            cap = int(np.prod(self.shape)) // 2 + 1
+            buf = np.zeros(cap, dtype=np.int64)
+            _check(lib().ppf_particles(self._h, float(threshold), ctypes.byref(st), buf.ctypes.data, cap,
+                                       ctypes.byref(n)))
+            d = st.as_dict()
+            d["volumes"] = np.sort(buf[:min(n.value, cap)])
+            return d
+        _check(lib().ppf_particles(self._h, float(threshold), ctypes.byref(st), None, 0, ctypes.byref(n)))
+        return st.as_dict()
 
     def autotune(self, trial_steps: int = 10) -> dict:
         t = Tune()

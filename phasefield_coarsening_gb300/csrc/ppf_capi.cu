@@ -17,6 +17,7 @@
 
 #include "ppf.h"
 #include "ppf_internal.h"
+#include "ppf_particles.h"
 #include "ppf_step_tma.h"
 
 using namespace ppf;
@@ -59,6 +60,9 @@ struct ppf_ctx {
     StepTune tune;        // launch choices of the fused step (grid, z chunk, unroll)
     unsigned long long wait_limit_ns;
     int inject;           // test hook: PPF_INJECT_*
+    int *plab, *pvol;     // particle labels / volumes (allocated on first use)
+    int64_t *plist;       // particle volume list (device), plist_cap entries
+    int64_t plist_cap;
     int64_t steps;
     int uploaded;
     Coef<float> kf;
@@ -240,6 +244,9 @@ extern "C" int ppf_destroy(ppf_ctx *c) {
     if (c->staging) cudaFree(c->staging);
     if (c->partials) cudaFree(c->partials);
     if (c->dres) cudaFree(c->dres);
+    if (c->plab) cudaFree(c->plab);
+    if (c->pvol) cudaFree(c->pvol);
+    if (c->plist) cudaFree(c->plist);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
     return PPF_OK;
@@ -520,6 +527,58 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
         best->roll = win.roll;
         best->grid = win.grid;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
+    }
+    return PPF_OK;
+}
+
+extern "C" int ppf_particles(ppf_ctx *c, double threshold, ppf_particle_stats *out, int64_t *volumes,
+                             int64_t capacity, int64_t *nvolumes) {
+    if (!c || !out) return seterr(PPF_EINVAL, "null argument");
+    if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
+    if (volumes && capacity < 0) return seterr(PPF_EINVAL, "negative capacity");
+    const int64_t cells = (int64_t)c->nz * c->ny * c->nx;
+    if (cells >= ((int64_t)1 << 31)) return seterr(PPF_EINVAL, "particle labels hold at most 2^31-1 cells");
+    if (!c->plab) CU(cudaMalloc(&c->plab, (size_t)cells * sizeof(int)));
+    if (!c->pvol) CU(cudaMalloc(&c->pvol, (size_t)cells * sizeof(int)));
+    int64_t cap = volumes ? capacity : 0;
+    if (cap > 0 && cap > c->plist_cap) {
+        if (c->plist) cudaFree(c->plist);
+        c->plist = nullptr;
+        c->plist_cap = 0;
+        CU(cudaMalloc(&c->plist, (size_t)cap * sizeof(int64_t) + 64));
+        c->plist_cap = cap;
+    }
+    int nb = (int)((cells + 255) / 256);
+    if (nb > 8 * c->num_sms) nb = 8 * c->num_sms;
+    int rc = ensure_partials(c, 5 * nb + 8);
+    if (rc) return rc;
+    unsigned long long *nlist = c->plist ? (unsigned long long *)(c->plist + c->plist_cap) : nullptr;
+    double *dout = c->dres + 8;
+    if (c->prec == PPF_F32)
+        CU(launch_particles<float>(c->g, (const float *)c->fld[c->cur_eta][0], threshold, c->plab, c->pvol,
+                                   c->partials, nb, c->p.dx, dout, cap > 0 ? c->plist : nullptr, cap, nlist, c->derr,
+                                   c->stream));
+    else
+        CU(launch_particles<double>(c->g, (const double *)c->fld[c->cur_eta][0], threshold, c->plab, c->pvol,
+                                    c->partials, nb, c->p.dx, dout, cap > 0 ? c->plist : nullptr, cap, nlist,
+                                    c->derr, c->stream));
+    double h[5];
+    unsigned long long hn = 0;
+    CU(cudaMemcpyAsync(h, dout, 5 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (cap > 0) CU(cudaMemcpyAsync(&hn, nlist, sizeof hn, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    rc = check_device_error(c);
+    if (rc) return rc;
+    const double dx = c->p.dx;
+    out->count = (int64_t)h[0];
+    out->mean_radius = h[0] > 0 ? h[1] / h[0] / dx : 0.0;
+    out->solid_volume = h[2] * dx * dx * dx;
+    out->largest_volume = h[3] * dx * dx * dx;
+    out->interface_area = h[4] * dx * dx;
+    if (nvolumes) *nvolumes = (int64_t)h[0];
+    if (cap > 0) {
+        const int64_t m = (int64_t)hn < cap ? (int64_t)hn : cap;
+        CU(cudaMemcpy(volumes, c->plist, (size_t)m * sizeof(int64_t), cudaMemcpyDeviceToHost));
     }
     return PPF_OK;
 }

@@ -1,0 +1,80 @@
+"""Particle analysis: the oracle's union-find on CPU, and the GPU labelling
+(through the C-ABI) against it."""
+import numpy as np
+import pytest
+
+import oracle
+import phasefield_coarsening_gb300 as ppf
+from phasefield_coarsening_gb300 import ic
+
+
+def _slab_across_x_face(n=16):
+    e = np.zeros((n, n, n))
+    e[4:8, 4:8, :3] = 1.0      # touches x = 0
+    e[4:8, 4:8, -2:] = 1.0     # touches x = n-1
+    e[10:12, 10:12, 6:9] = 1.0
+    return e
+
+
+def test_oracle_joins_across_periodic_faces_only():
+    e = _slab_across_x_face()
+    p = oracle.particles(e, bc=0)
+    f = oracle.particles(e, bc=1)
+    assert p["count"] == 2 and f["count"] == 3
+    assert sorted(p["volumes"]) == [12, 80]
+    assert p["solid_volume"] == f["solid_volume"] == 92
+
+
+def test_oracle_mean_radius_of_spheres():
+    eS, _, _, info = ic.generate((48, 48, 48), radius=("uniform", 4, 8), count=10, seed=3)
+    p = oracle.particles(eS, bc=0)
+    assert p["count"] == 10
+    assert abs(p["mean_radius"] - info["mean_radius"]) < 0.05 * info["mean_radius"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("bc", [0, 1])
+def test_gpu_particles_match_oracle(precision, bc):
+    eS, eL, c, _ = ic.generate((40, 36, 70), radius=("uniform", 3, 7), count=25, seed=7 + bc)
+    with ppf.Simulation(eS.shape, bc=bc, precision=precision) as s:
+        s.upload(eS, eL, c)
+        g = s.particles(volumes=True)
+        field = s.download()[0]
+    o = oracle.particles(field, bc=bc)
+    assert g["count"] == o["count"] > 5
+    assert np.array_equal(g["volumes"], o["volumes"])
+    assert abs(g["mean_radius"] - o["mean_radius"]) <= 1e-12 * o["mean_radius"]
+    assert g["solid_volume"] == o["solid_volume"] and g["interface_area"] == o["interface_area"]
+    assert g["largest_volume"] == o["largest_volume"]
+
+
+@pytest.mark.gpu
+def test_gpu_particles_wrap_and_edge_cases():
+    e = _slab_across_x_face(16)
+    for bc, n in ((0, 2), (1, 3)):
+        with ppf.Simulation(e.shape, bc=bc) as s:
+            s.upload(e, 1.0 - e, np.full(e.shape, 0.9))
+            assert s.particles()["count"] == n
+    empty = np.zeros((8, 8, 8))
+    with ppf.Simulation(empty.shape) as s:
+        s.upload(empty, 1.0 - empty, np.full(empty.shape, 0.9))
+        st = s.particles(volumes=True)
+        assert st["count"] == 0 and st["mean_radius"] == 0.0 and len(st["volumes"]) == 0
+    full = np.ones((8, 8, 8))
+    with ppf.Simulation(full.shape) as s:
+        s.upload(full, 1.0 - full, np.full(full.shape, 0.476))
+        st = s.particles()
+        assert st["count"] == 1 and st["solid_volume"] == 512 and st["interface_area"] == 0
+
+
+@pytest.mark.gpu
+def test_fp32_mean_radius_within_half_percent_of_fp64():
+    """The FP32 path against the FP64 path (itself pinned to the oracle) on
+    the 64^3 sphere workload after 2000 steps: R-bar within 0.5 %."""
+    from phasefield_coarsening_gb300 import validate
+    r = validate.compare((64, 64, 64), "spheres64_uniform4to8", steps=2000, seed=0)
+    print(r)
+    assert r["rbar_rel_err"] <= 5e-3
+    assert r["count_fp32"] == r["count_fp64"]
+    assert abs(r["mass_drift_fp32"]) <= 1e-8

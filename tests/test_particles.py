@@ -77,4 +77,9 @@ def test_fp32_mean_radius_within_half_percent_of_fp64():
     print(r)
     assert r["rbar_rel_err"] <= 5e-3
     assert r["count_fp32"] == r["count_fp64"]
-    assert abs(r["mass_drift_fp32"]) <= 1e-8
+    # FP32 storage loses increments below half an ulp of c, and the ulp is
+    # twice as large in the liquid (c ~ 0.999) as in the solid (c ~ 0.476):
+    # a slow systematic drift, 1.5e-8 relative here (6.8e-8 after 10k steps
+    # at 256^3); the FP64 path conserves to round-off
+    assert abs(r["mass_drift_fp32"]) <= 5e-8
+    assert abs(r["mass_drift_fp64"]) <= 1e-13

@@ -221,6 +221,32 @@ int ppf_autotune(ppf_ctx *ctx, int trial_steps, ppf_tune *best);
 int ppf_observe_noalloc(int nz, int ny, int nx, const ppf_params *p, int bc, const double *etaS,
                         const double *etaL, const double *c, double *out, void *stream);
 
+/* Ensembles: many independent domains of different sizes (same parameters,
+ * BC and precision) advanced together -- one persistent launch of the
+ * fused step per time step covers every domain's work items, and runs of
+ * steps replay a captured CUDA graph.  No counterpart in the reference,
+ * which runs one domain per program.  Each domain is an ordinary context
+ * (ppf_ensemble_domain) for uploads, downloads and reductions; stepping
+ * goes through the ensemble only. */
+typedef struct ppf_ensemble ppf_ensemble;
+
+/* dims: n triples (nz, ny, nx). */
+int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, int bc, int precision,
+                        ppf_ensemble **out);
+int ppf_ensemble_destroy(ppf_ensemble *ens);
+int ppf_ensemble_domain(ppf_ensemble *ens, int d, ppf_ctx **ctx);
+int ppf_ensemble_upload(ppf_ensemble *ens, int d, const double *etaS, const double *etaL, const double *c);
+int ppf_ensemble_download(ppf_ensemble *ens, int d, double *etaS, double *etaL, double *c);
+/* nsteps full steps of every domain (all domains need an uploaded state);
+ * the last step's increment sums go to each domain's ppf_reduce. */
+int ppf_ensemble_step(ppf_ensemble *ens, int64_t nsteps);
+int ppf_ensemble_reduce(ppf_ensemble *ens, int d, ppf_stats *out);
+int ppf_ensemble_sync(ppf_ensemble *ens);
+int ppf_ensemble_get_tune(const ppf_ensemble *ens, ppf_tune *out);
+int ppf_ensemble_set_tune(ppf_ensemble *ens, const ppf_tune *t);
+/* Like ppf_autotune, over the whole ensemble (states kept). */
+int ppf_ensemble_autotune(ppf_ensemble *ens, int trial_steps, ppf_tune *best);
+
 /* Message for the calling thread's last failure ("" if none). */
 const char *ppf_last_error(void);
 

@@ -28,7 +28,10 @@ EXPORTS = (
     "ppf_params_default", "ppf_params_derive", "ppf_create", "ppf_destroy", "ppf_get_dims", "ppf_set_stream",
     "ppf_upload", "ppf_download", "ppf_upload_device", "ppf_download_device", "ppf_step", "ppf_step_c_only",
     "ppf_reduce", "ppf_sync", "ppf_set_wait_limit", "ppf_debug_inject", "ppf_get_tune", "ppf_set_tune",
-    "ppf_autotune", "ppf_observe_noalloc", "ppf_particles", "ppf_last_error", "ppf_version",
+    "ppf_autotune", "ppf_observe_noalloc", "ppf_particles", "ppf_ensemble_create", "ppf_ensemble_destroy",
+    "ppf_ensemble_domain", "ppf_ensemble_upload", "ppf_ensemble_download", "ppf_ensemble_step",
+    "ppf_ensemble_reduce", "ppf_ensemble_sync", "ppf_ensemble_get_tune", "ppf_ensemble_set_tune",
+    "ppf_ensemble_autotune", "ppf_last_error", "ppf_version",
     "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_last_error",
 )
 
@@ -116,6 +119,18 @@ def lib() -> ctypes.CDLL:
         L.ppf_particles.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ParticleStats),
                                     ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
         L.ppf_get_dims.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 3
+        L.ppf_ensemble_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(Params),
+                                          ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        for n in ("ppf_ensemble_destroy", "ppf_ensemble_sync"):
+            getattr(L, n).argtypes = [ctypes.c_void_p]
+        L.ppf_ensemble_domain.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        for n in ("ppf_ensemble_upload", "ppf_ensemble_download"):
+            getattr(L, n).argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
+        L.ppf_ensemble_step.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+        L.ppf_ensemble_reduce.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Stats)]
+        L.ppf_ensemble_get_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
+        L.ppf_ensemble_set_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
+        L.ppf_ensemble_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Tune)]
         L.ppf_h5_dims.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.ppf_h5_read3d.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _dp,
                                     ctypes.c_int64]
@@ -257,6 +272,79 @@ class Simulation:
         return s.as_dict()
 
 
+class Ensemble:
+    """Host-side mirror of a ppf_ensemble: independent domains of different
+    sizes stepped together by one persistent launch per time step."""
+
+    def __init__(self, shapes, params: Params | None = None, bc="periodic", precision="f32"):
+        self.shapes = [tuple(int(v) for v in sh) for sh in shapes]
+        self.params = params if params is not None else params_default()
+        dims = (ctypes.c_int * (3 * len(self.shapes)))(*[v for sh in self.shapes for v in sh])
+        h = ctypes.c_void_p()
+        _check(lib().ppf_ensemble_create(len(self.shapes), dims, ctypes.byref(self.params), _BC[bc], _PREC[precision],
+                                         ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ppf_ensemble_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.shapes)
+
+    def upload(self, d, etaS, etaL, c):
+        a = [_c64(x) for x in (etaS, etaL, c)]
+        if any(x.shape != self.shapes[d] for x in a):
+            raise ValueError("field shape does not match the domain")
+        _check(lib().ppf_ensemble_upload(self._h, int(d), *[x.ctypes.data for x in a]))
+
+    def download(self, d):
+        out = [np.empty(self.shapes[d], np.float64) for _ in range(3)]
+        _check(lib().ppf_ensemble_download(self._h, int(d), *[x.ctypes.data for x in out]))
+        return tuple(out)
+
+    def step(self, n=1):
+        _check(lib().ppf_ensemble_step(self._h, int(n)))
+
+    def sync(self):
+        _check(lib().ppf_ensemble_sync(self._h))
+
+    def reduce(self, d) -> dict:
+        s = Stats()
+        _check(lib().ppf_ensemble_reduce(self._h, int(d), ctypes.byref(s)))
+        return s.as_dict()
+
+    def particles(self, d, threshold=0.5) -> dict:
+        ctx = ctypes.c_void_p()
+        _check(lib().ppf_ensemble_domain(self._h, int(d), ctypes.byref(ctx)))
+        st = ParticleStats()
+        _check(lib().ppf_particles(ctx, float(threshold), ctypes.byref(st), None, 0, None))
+        return st.as_dict()
+
+    def get_tune(self) -> dict:
+        t = Tune()
+        _check(lib().ppf_ensemble_get_tune(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tune(self, zc: int, roll: int = 1):
+        t = Tune(int(zc), int(roll), 0, 0.0)
+        _check(lib().ppf_ensemble_set_tune(self._h, ctypes.byref(t)))
+
+    def autotune(self, trial_steps: int = 5) -> dict:
+        t = Tune()
+        _check(lib().ppf_ensemble_autotune(self._h, int(trial_steps), ctypes.byref(t)))
+        return t.as_dict()
+
+
 # ---------------------------------------------------------------- HDF5 ----
 
 def h5_dims(path: str, name: str):
@@ -300,6 +388,6 @@ def write_fields(path: str, etaS, etaL, c, dtype="f64", chunk=None):
     h5_write(path, {"etaS": etaS, "etaL": etaL, "c": c}, dtype=dtype, chunk=chunk)
 
 
-__all__ = ["Simulation", "Params", "Stats", "Derived", "PPFError", "params_default", "derive", "lib",
+__all__ = ["Simulation", "Ensemble", "Params", "Stats", "Derived", "PPFError", "params_default", "derive", "lib",
            "h5_read", "h5_write", "h5_dims", "read_fields", "write_fields", "BC_PERIODIC", "BC_NOFLUX",
            "F64", "F32", "LIB_PATH", "EXE_PATH", "EXPORTS"]

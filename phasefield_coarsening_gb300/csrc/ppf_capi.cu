@@ -41,35 +41,8 @@ int ppf::set_last_error(int code, const char *msg) { return seterr(code, "%s", m
             return seterr(PPF_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
-struct ppf_ctx {
-    int nz, ny, nx, bc, prec;
-    ppf_params p;
-    ppf_derived d;
-    Geom g;
-    int dev, num_sms;
-    cudaStream_t own, stream;
-    void *state;          // one allocation: 2 buffers x 3 fields x g.total elements
-    void *fld[2][3];      // [buffer][etaS, etaL, c]
-    int cur_eta, cur_c;   // buffer holding the current eta / c
-    double *staging;      // 3 * cells doubles, compact [z][y][x]
-    double *partials;     // per-CTA partial sums
-    int partials_cap;     // in doubles
-    double *dres;         // device results: [0..2] increments, [3..7] observables
-    int *derr;            // device error word set by a kernel whose bounded wait ran out
-    CUtensorMap maps[2][3];   // TMA maps of the fields of both buffers
-    StepTune tune;        // launch choices of the fused step (grid, z chunk, unroll)
-    unsigned long long wait_limit_ns;
-    int inject;           // test hook: PPF_INJECT_*
-    int *plab, *pvol;     // particle labels / volumes (allocated on first use)
-    int64_t *plist;       // particle volume list (device), plist_cap entries
-    int64_t plist_cap;
-    int64_t steps;
-    int uploaded;
-    Coef<float> kf;
-    Coef<double> kd;
-    int eqA;              // AS == AL: the mu reciprocal is a constant
-    CoefD cd;
-};
+#include "ppf_ctx.h"
+
 
 extern "C" void ppf_params_default(ppf_params *p) {
     if (!p) return;
@@ -134,7 +107,7 @@ static Coef<T> make_coef(const ppf_params &p, const ppf_derived &d) {
     return k;
 }
 
-static int check_device_error(ppf_ctx *c);
+int check_device_error(ppf_ctx *c);
 
 static Fields<float> ff(ppf_ctx *c, int be, int bc_) {
     return {(float *)c->fld[be][0], (float *)c->fld[be][1], (float *)c->fld[bc_][2]};
@@ -147,7 +120,7 @@ static Fields<const T> cst(Fields<T> f) {
     return {f.eS, f.eL, f.c};
 }
 
-static int ensure_partials(ppf_ctx *c, int ndoubles) {
+int ensure_partials(ppf_ctx *c, int ndoubles) {
     if (ndoubles <= c->partials_cap) return PPF_OK;
     if (c->partials) cudaFree(c->partials);
     c->partials = nullptr;
@@ -267,7 +240,7 @@ extern "C" int ppf_set_stream(ppf_ctx *c, void *stream) {
     return PPF_OK;
 }
 
-static int do_pack(ppf_ctx *c) {
+int do_pack(ppf_ctx *c) {
     c->cur_eta = 0;
     c->cur_c = 0;
     if (c->prec == PPF_F32) CU(launch_pack<float>(c->g, c->staging, ff(c, 0, 0), c->stream));
@@ -302,7 +275,7 @@ extern "C" int ppf_upload_device(ppf_ctx *c, const double *etaS, const double *e
     return PPF_OK;
 }
 
-static int do_unpack(ppf_ctx *c) {
+int do_unpack(ppf_ctx *c) {
     if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
     if (c->prec == PPF_F32)
         CU(launch_unpack<float>(c->g, cst(ff(c, c->cur_eta, c->cur_c)), c->staging, c->stream));
@@ -337,7 +310,7 @@ extern "C" int ppf_download_device(ppf_ctx *c, double *etaS, double *etaL, doubl
 
 // Reads and clears the device error word; PPF_ETIMEOUT when a kernel's
 // bounded wait ran out since the last check.
-static int check_device_error(ppf_ctx *c) {
+int check_device_error(ppf_ctx *c) {
     int h = 0;
     CU(cudaMemcpyAsync(&h, c->derr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));

@@ -1,0 +1,378 @@
+// ppf_ensemble.cu -- many independent domains of different sizes advanced
+// together: one persistent launch of the fused step per time step covers
+// the work items of every domain (the MULTI variant of step_tma_kernel,
+// reading each item's geometry and TMA descriptors from a device table),
+// and runs of steps are replayed from a captured CUDA graph.
+//
+// No counterpart in the reference, which runs one domain per program.
+// Each domain is an ordinary ppf_ctx (its own buffers, descriptors,
+// uploads, downloads and reductions); the ensemble only owns the table, the
+// per-item partial sums, the graph and the launch choices.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "ppf_ctx.h"
+
+using namespace ppf;
+
+namespace {
+
+int err_(int code, const char *fmt, ...) {
+    char msg[256];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof msg, fmt, ap);
+    va_end(ap);
+    return set_last_error(code, msg);
+}
+
+#define ECU(call)                                                                                 \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return err_(PPF_ECUDA, "%s: %s", #call, cudaGetErrorString(e_));   \
+    } while (0)
+
+// per-domain sums of the per-item increment partials (deterministic order)
+__global__ void domain_sums(const DomainDesc *__restrict__ table, const double *__restrict__ partials,
+                            double *const *__restrict__ dres) {
+    const DomainDesc &d = table[blockIdx.x];
+    __shared__ double red[3][128];
+    double a[3] = {0, 0, 0};
+    for (int i = threadIdx.x; i < d.nitems; i += blockDim.x)
+        for (int v = 0; v < 3; ++v) a[v] += partials[(int64_t)(d.item0 + i) * 3 + v];
+    for (int v = 0; v < 3; ++v) red[v][threadIdx.x] = a[v];
+    __syncthreads();
+    for (int h = 64; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int v = 0; v < 3; ++v) red[v][threadIdx.x] += red[v][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int v = 0; v < 3; ++v) dres[blockIdx.x][v] = red[v][0];
+}
+
+}  // namespace
+
+struct ppf_ensemble {
+    int n, prec, bc, eqA;
+    std::vector<ppf_ctx *> dom;
+    DomainDesc *dtable;          // device
+    double **ddres;              // device: each domain's dres pointer
+    double *partials;            // 3 doubles per work item
+    int partials_cap;
+    int items, grid, zc, roll;
+    int parity;                  // buffer holding the current state of every domain
+    int64_t steps;
+    cudaStream_t stream;
+    cudaGraphExec_t graph;       // kGraphSteps plain steps, starting and ending at parity 0
+    int graph_ok;
+    int num_sms;
+};
+
+static constexpr int kGraphSteps = 16;
+
+static int build_table(ppf_ensemble *e) {
+    int tx = 0, ty = 0;
+    if (e->prec == PPF_F32) step_tile<float>(&tx, &ty);
+    else step_tile<double>(&tx, &ty);
+    std::vector<DomainDesc> h((size_t)e->n);
+    int64_t item0 = 0;
+    for (int d = 0; d < e->n; ++d) {
+        ppf_ctx *c = e->dom[(size_t)d];
+        DomainDesc &t = h[(size_t)d];
+        memset(&t, 0, sizeof t);
+        for (int b = 0; b < 2; ++b)
+            for (int f = 0; f < 3; ++f) {
+                t.maps[b][f] = c->maps[b][f];
+                t.fld[b][f] = c->fld[b][f];
+            }
+        t.g = c->g;
+        t.ntx = (c->nx + tx - 1) / tx;
+        t.nty = (c->ny + ty - 1) / ty;
+        t.zc = e->zc < c->nz ? e->zc : c->nz;
+        t.nc = (c->nz + t.zc - 1) / t.zc;
+        t.item0 = (int)item0;
+        t.nitems = t.ntx * t.nty * t.nc;
+        item0 += t.nitems;
+    }
+    if (item0 > ((int64_t)1 << 30)) return err_(PPF_EINVAL, "ensemble has too many work items");
+    e->items = (int)item0;
+    e->grid = e->prec == PPF_F32 ? tma_grid_items<float>(item0, e->num_sms) : tma_grid_items<double>(item0, e->num_sms);
+    if (e->grid < 1) return err_(PPF_ECUDA, "no launch shape for the ensemble");
+    ECU(cudaMemcpyAsync(e->dtable, h.data(), h.size() * sizeof(DomainDesc), cudaMemcpyHostToDevice, e->stream));
+    if (3 * e->items > e->partials_cap) {
+        if (e->partials) cudaFree(e->partials);
+        e->partials = nullptr;
+        ECU(cudaMalloc(&e->partials, (size_t)3 * e->items * sizeof(double)));
+        e->partials_cap = 3 * e->items;
+    }
+    ECU(cudaStreamSynchronize(e->stream));
+    if (e->graph_ok) cudaGraphExecDestroy(e->graph);
+    e->graph_ok = 0;
+    return PPF_OK;
+}
+
+static int launch_one(ppf_ensemble *e, bool stats) {
+    const int inj = 0;
+    (void)inj;
+    ppf_ctx *c0 = e->dom[0];
+    cudaError_t r;
+    if (e->prec == PPF_F32)
+        r = launch_step_multi<float>(e->dtable, e->n, e->items, c0->kf, false, e->eqA, e->parity,
+                                     stats ? e->partials : nullptr, e->grid, e->roll, c0->derr, c0->wait_limit_ns,
+                                     e->stream);
+    else
+        r = launch_step_multi<double>(e->dtable, e->n, e->items, c0->kd, false, e->eqA, e->parity,
+                                      stats ? e->partials : nullptr, e->grid, e->roll, c0->derr, c0->wait_limit_ns,
+                                      e->stream);
+    if (r != cudaSuccess) return err_(PPF_ECUDA, "ensemble step launch: %s", cudaGetErrorString(r));
+    e->parity ^= 1;
+    return PPF_OK;
+}
+
+static int ensure_graph(ppf_ensemble *e) {
+    if (e->graph_ok) return PPF_OK;
+    cudaGraph_t g;
+    const int p0 = e->parity;
+    e->parity = 0;
+    ECU(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = PPF_OK;
+    for (int s = 0; s < kGraphSteps && rc == PPF_OK; ++s) rc = launch_one(e, false);
+    cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+    e->parity = p0;
+    if (rc) return rc;
+    if (ce != cudaSuccess) return err_(PPF_ECUDA, "graph capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&e->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return err_(PPF_ECUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    e->graph_ok = 1;
+    return PPF_OK;
+}
+
+extern "C" int ppf_ensemble_destroy(ppf_ensemble *e) {
+    if (!e) return PPF_OK;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->graph_ok) cudaGraphExecDestroy(e->graph);
+    for (ppf_ctx *c : e->dom) ppf_destroy(c);
+    if (e->dtable) cudaFree(e->dtable);
+    if (e->ddres) cudaFree(e->ddres);
+    if (e->partials) cudaFree(e->partials);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return PPF_OK;
+}
+
+extern "C" int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, int bc, int precision,
+                                   ppf_ensemble **out) {
+    if (!out || !dims || n < 1 || n > 4096) return err_(PPF_EINVAL, "ensemble: bad arguments");
+    *out = nullptr;
+    ppf_ensemble *e = new (std::nothrow) ppf_ensemble();
+    if (!e) return err_(PPF_ENOMEM, "host allocation failed");
+    e->n = n;
+    e->prec = precision;
+    e->bc = bc;
+    e->zc = 32;
+    e->roll = 1;
+    int rc = PPF_OK;
+    for (int d = 0; d < n && rc == PPF_OK; ++d) {
+        ppf_ctx *c = nullptr;
+        rc = ppf_create(dims[3 * d], dims[3 * d + 1], dims[3 * d + 2], p, bc, precision, &c);
+        if (rc == PPF_OK) e->dom.push_back(c);
+    }
+    if (rc) {
+        ppf_ensemble_destroy(e);
+        return rc;
+    }
+    ppf_ctx *c0 = e->dom[0];
+    e->num_sms = c0->num_sms;
+    e->eqA = c0->eqA;
+    cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->dtable, (size_t)n * sizeof(DomainDesc));
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->ddres, (size_t)n * sizeof(double *));
+    if (ce != cudaSuccess) {
+        ppf_ensemble_destroy(e);
+        return err_(PPF_ECUDA, "ensemble setup: %s", cudaGetErrorString(ce));
+    }
+    std::vector<double *> h((size_t)n);
+    for (int d = 0; d < n; ++d) {
+        h[(size_t)d] = e->dom[(size_t)d]->dres;
+        e->dom[(size_t)d]->stream = e->stream;   // one stream orders every domain's work
+    }
+    ce = cudaMemcpy(e->ddres, h.data(), (size_t)n * sizeof(double *), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+        ppf_ensemble_destroy(e);
+        return err_(PPF_ECUDA, "ensemble setup: %s", cudaGetErrorString(ce));
+    }
+    rc = build_table(e);
+    if (rc) {
+        ppf_ensemble_destroy(e);
+        return rc;
+    }
+    *out = e;
+    return PPF_OK;
+}
+
+static int check_domain(ppf_ensemble *e, int d) {
+    if (!e) return err_(PPF_EINVAL, "null ensemble");
+    if (d < 0 || d >= e->n) return err_(PPF_EINVAL, "domain %d out of range [0, %d)", d, e->n);
+    return PPF_OK;
+}
+
+extern "C" int ppf_ensemble_domain(ppf_ensemble *e, int d, ppf_ctx **ctx) {
+    int rc = check_domain(e, d);
+    if (rc) return rc;
+    if (!ctx) return err_(PPF_EINVAL, "null argument");
+    *ctx = e->dom[(size_t)d];
+    return PPF_OK;
+}
+
+extern "C" int ppf_ensemble_upload(ppf_ensemble *e, int d, const double *etaS, const double *etaL, const double *c) {
+    int rc = check_domain(e, d);
+    if (rc) return rc;
+    if (e->parity != 0) {
+        // the domains are stepped together; a fresh upload lands in buffer 0,
+        // so bring every other domain to buffer 0 first
+        for (ppf_ctx *x : e->dom)
+            if (x->uploaded && (rc = do_unpack(x)) == PPF_OK) rc = do_pack(x);
+        if (rc) return rc;
+        e->parity = 0;
+    }
+    return ppf_upload(e->dom[(size_t)d], etaS, etaL, c);
+}
+
+extern "C" int ppf_ensemble_download(ppf_ensemble *e, int d, double *etaS, double *etaL, double *c) {
+    int rc = check_domain(e, d);
+    if (rc) return rc;
+    return ppf_download(e->dom[(size_t)d], etaS, etaL, c);
+}
+
+extern "C" int ppf_ensemble_reduce(ppf_ensemble *e, int d, ppf_stats *out) {
+    int rc = check_domain(e, d);
+    if (rc) return rc;
+    return ppf_reduce(e->dom[(size_t)d], out);
+}
+
+static int run(ppf_ensemble *e, int64_t nsteps) {
+    for (ppf_ctx *x : e->dom)
+        if (!x->uploaded) return err_(PPF_ESTATE, "every domain needs an uploaded state");
+    int rc = PPF_OK;
+    int64_t left = nsteps;
+    // whole graphs of plain steps (they start at buffer 0) while at least one
+    // step remains for the statistics step
+    if (left - 1 > kGraphSteps && e->parity == 1) {
+        if ((rc = launch_one(e, false)) != PPF_OK) return rc;
+        --left;
+    }
+    if (left - 1 >= kGraphSteps && e->parity == 0) {
+        if ((rc = ensure_graph(e)) != PPF_OK) return rc;
+        while (left - 1 >= kGraphSteps) {
+            ECU(cudaGraphLaunch(e->graph, e->stream));
+            left -= kGraphSteps;
+        }
+    }
+    for (; left > 0 && rc == PPF_OK; --left) rc = launch_one(e, left == 1);
+    if (rc) return rc;
+    domain_sums<<<e->n, 128, 0, e->stream>>>(e->dtable, e->partials, e->ddres);
+    ECU(cudaGetLastError());
+    for (ppf_ctx *x : e->dom) {
+        x->cur_eta = x->cur_c = e->parity;
+        x->steps += nsteps;
+    }
+    e->steps += nsteps;
+    return PPF_OK;
+}
+
+extern "C" int ppf_ensemble_step(ppf_ensemble *e, int64_t nsteps) {
+    if (!e) return err_(PPF_EINVAL, "null ensemble");
+    if (nsteps < 0) return err_(PPF_EINVAL, "negative step count");
+    if (nsteps == 0) return PPF_OK;
+    return run(e, nsteps);
+}
+
+extern "C" int ppf_ensemble_sync(ppf_ensemble *e) {
+    if (!e) return err_(PPF_EINVAL, "null ensemble");
+    ECU(cudaStreamSynchronize(e->stream));
+    return check_device_error(e->dom[0]);
+}
+
+extern "C" int ppf_ensemble_get_tune(const ppf_ensemble *e, ppf_tune *t) {
+    if (!e || !t) return err_(PPF_EINVAL, "null argument");
+    t->zc = e->zc;
+    t->roll = e->roll;
+    t->grid = e->grid;
+    t->us_per_step = 0;
+    return PPF_OK;
+}
+
+extern "C" int ppf_ensemble_set_tune(ppf_ensemble *e, const ppf_tune *t) {
+    if (!e || !t) return err_(PPF_EINVAL, "null argument");
+    if (t->roll != 1 && t->roll != 3) return err_(PPF_EINVAL, "roll must be 1 or 3");
+    if (t->zc < 1) return err_(PPF_EINVAL, "zc must be >= 1");
+    ECU(cudaStreamSynchronize(e->stream));
+    e->zc = t->zc;
+    e->roll = t->roll;
+    return build_table(e);
+}
+
+extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune *best) {
+    if (!e) return err_(PPF_EINVAL, "null ensemble");
+    if (trial_steps < 1) trial_steps = 1;
+    for (ppf_ctx *x : e->dom)
+        if (!x->uploaded) return err_(PPF_ESTATE, "autotuning needs every domain's state");
+    int rc = PPF_OK;
+    // keep every domain's state: save it, try the choices, restore it
+    for (ppf_ctx *x : e->dom)
+        if ((rc = do_unpack(x)) != PPF_OK) return rc;
+    const int zcs[] = {8, 16, 24, 32, 48, 64, 128};
+    const int keep_zc = e->zc, keep_roll = e->roll;
+    const int64_t keep_steps = e->steps;
+    int best_zc = keep_zc, best_roll = keep_roll;
+    float best_ms = -1.0f;
+    cudaEvent_t t0, t1;
+    ECU(cudaEventCreate(&t0));
+    ECU(cudaEventCreate(&t1));
+    for (int r = 0; r < 2 && rc == PPF_OK; ++r)
+        for (int zc : zcs) {
+            e->zc = zc;
+            e->roll = r == 0 ? 1 : 3;
+            if ((rc = build_table(e)) != PPF_OK) break;
+            for (int s = 0; s < 2 && rc == PPF_OK; ++s) rc = launch_one(e, false);     // warm-up
+            if (rc) break;
+            cudaEventRecord(t0, e->stream);
+            for (int s = 0; s < trial_steps && rc == PPF_OK; ++s) rc = launch_one(e, false);
+            cudaEventRecord(t1, e->stream);
+            if (cudaEventSynchronize(t1) != cudaSuccess) { rc = err_(PPF_ECUDA, "event timing failed"); break; }
+            if ((rc = check_device_error(e->dom[0])) != PPF_OK) break;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, t0, t1);
+            if (best_ms < 0 || ms < best_ms) { best_ms = ms; best_zc = e->zc; best_roll = e->roll; }
+        }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    e->zc = rc == PPF_OK ? best_zc : keep_zc;
+    e->roll = rc == PPF_OK ? best_roll : keep_roll;
+    int rc2 = build_table(e);
+    for (ppf_ctx *x : e->dom)
+        if (rc2 == PPF_OK) {
+            const int64_t s0 = x->steps;
+            rc2 = do_pack(x);
+            x->steps = s0;
+        }
+    e->parity = 0;
+    e->steps = keep_steps;
+    if (rc2 == PPF_OK && cudaStreamSynchronize(e->stream) != cudaSuccess) rc2 = err_(PPF_ECUDA, "restore failed");
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (best) {
+        best->zc = e->zc;
+        best->roll = e->roll;
+        best->grid = e->grid;
+        best->us_per_step = best_ms * 1000.0 / trial_steps;
+    }
+    return PPF_OK;
+}

@@ -276,27 +276,7 @@ __device__ __forceinline__ void store_ghosts(const Geom &g, const Fields<T> &o, 
 // Work items are (z chunk, x-y tile) pairs in chunk-major order, dealt
 // round-robin to the persistent CTAs: CTAs resident at the same time march
 // the same z window of neighbouring tiles, so the halo rows one tile reads
-// from its neighbours' data are still in L2.  A walker yields the load
-// sequence of one CTA: for each of its items, planes z0-1 .. z1.
-struct ItemWalk {
-    int item, stride, nitems, ntiles, zc, nz;
-    int tile, z0, z1, pz;
-    __device__ __forceinline__ void start(int first, int stride_, int nitems_, int ntiles_, int zc_, int nz_) {
-        item = first; stride = stride_; nitems = nitems_; ntiles = ntiles_; zc = zc_; nz = nz_;
-        set();
-    }
-    __device__ __forceinline__ void set() {
-        if (item >= nitems) { tile = -1; return; }
-        const int c = item / ntiles;
-        tile = item - c * ntiles;
-        z0 = c * zc;
-        z1 = min(nz, z0 + zc);
-        pz = z0 - 1;
-    }
-    __device__ __forceinline__ bool valid() const { return tile >= 0; }
-    __device__ __forceinline__ void next_item() { item += stride; set(); }
-    __device__ __forceinline__ void advance() { if (++pz > z1) next_item(); }
-};
+// from its neighbours' data are still in L2.
 
 // Registers of the own cells of one plane, as pairs (cell i, cell i+H) of
 // the thread's column of CY = 2H cells: with that pairing the y neighbours
@@ -306,12 +286,47 @@ struct PlaneRegs {
     V2<T> S[H], L[H], mu[H], M[H], c[H], d[H];
 };
 
-template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL>
+// A work item: one tile column segment of one domain.
+struct Item {
+    int dom, tile, z0, z1;
+};
+
+// Work item `item` of the launch.  Single domain: (z chunk, tile) in
+// chunk-major order.  Ensemble (MULTI): the items of each domain are
+// contiguous, chunk-major within the domain.
+template <bool MULTI>
+__device__ __forceinline__ Item item_at(int item, int ntiles, int zc, int nz, const DomainDesc *table, int ndom) {
+    Item it;
+    if (!MULTI) {
+        const int c = item / ntiles;
+        it.dom = 0;
+        it.tile = item - c * ntiles;
+        it.z0 = c * zc;
+        it.z1 = min(nz, it.z0 + zc);
+        return it;
+    }
+    int lo = 0, hi = ndom - 1;                 // last domain with item0 <= item
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (table[mid].item0 <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    const DomainDesc &d = table[lo];
+    const int li = item - d.item0, nt = d.ntx * d.nty;
+    const int c = li / nt;
+    it.dom = lo;
+    it.tile = li - c * nt;
+    it.z0 = c * d.zc;
+    it.z1 = min(d.g.nz, it.z0 + d.zc);
+    return it;
+}
+
+template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL, bool MULTI>
 __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
-                    const __grid_constant__ CUtensorMap mapC, Geom g, Coef<T> k, Fields<T> out, int ntx, int nty,
-                    int zc, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
-                    int inject_stall) {
+                    const __grid_constant__ CUtensorMap mapC, Geom g1, Coef<T> k, Fields<T> out1, int ntx1, int nty1,
+                    int zc1, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
+                    int inject_stall, const DomainDesc *__restrict__ table, int ndom, int mitems, int parity) {
     using G = TmaGeo<T>;
     constexpr int TX = G::TX, TY = G::TY, S = G::S, XH = G::XH, BX = G::BX, CY = G::CY;
     extern __shared__ __align__(128) unsigned char smem_dyn[];
@@ -324,8 +339,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = (warp % G::WX) * 32 + lane;        // own column in the tile
     const int ty0 = (warp / G::WX) * CY;              // first own row in the tile
-    const int ntiles = ntx * nty;
-    const int nitems = ntiles * ((g.nz + zc - 1) / zc);
+    const int ntiles1 = ntx1 * nty1;
+    const int nitems = MULTI ? mitems : ntiles1 * ((g1.nz + zc1 - 1) / zc1);
     const int ob = (ty0 + 1) * BX + tx + XH;          // shared offset of the first own cell
 
     double acc[3] = {0.0, 0.0, 0.0};
@@ -338,28 +353,44 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
         }
         __syncthreads();
 
-        // producer (thread 0): next load to issue, its stage, loads issued
-        ItemWalk prod;
-        prod.start(blockIdx.x, gridDim.x, nitems, ntiles, zc, g.nz);
+        // producer (thread 0): walks the same items and planes as the consumers,
+        // S-2 loads ahead
+        int p_item = blockIdx.x, p_pz = 0;
+        Item p_it;
+        auto p_set = [&]() {
+            if (p_item < nitems) {
+                p_it = item_at<MULTI>(p_item, ntiles1, zc1, g1.nz, table, ndom);
+                p_pz = p_it.z0 - 1;
+            }
+        };
+        p_set();
         int ist = 0, issued = 0;
         auto issue = [&]() {
             const uint32_t bar = smem_u32(&sm.bar[ist]);
-            const int bx = prod.tile % ntx, by = prod.tile / ntx;
-            const int xs = bx * TX + g.xoff - XH;     // storage x of the box start (16-byte aligned)
+            const int ntx = MULTI ? table[p_it.dom].ntx : ntx1;
+            const int xoff = MULTI ? table[p_it.dom].g.xoff : g1.xoff;
+            const CUtensorMap *mS = MULTI ? &table[p_it.dom].maps[parity][0] : &mapS;
+            const CUtensorMap *mL = MULTI ? &table[p_it.dom].maps[parity][1] : &mapL;
+            const CUtensorMap *mC = MULTI ? &table[p_it.dom].maps[parity][2] : &mapC;
+            const int bx = p_it.tile % ntx, by = p_it.tile / ntx;
+            const int xs = bx * TX + xoff - XH;       // storage x of the box start (16-byte aligned)
             const int ys = by * TY;                    // storage y of interior y0-1
-            const int zs = prod.pz + 1;                // storage z of the plane
+            const int zs = p_pz + 1;                   // storage z of the plane
             uint32_t bytes = 3u * (uint32_t)G::BOX_BYTES;
             if (inject_stall && issued == 1) bytes += 16u;   // test hook: this phase can never complete
             mbar_expect_tx(bar, bytes);
-            tma_load_3d(smem_u32(sm.raw[ist][0]), &mapS, xs, ys, zs, bar);
-            tma_load_3d(smem_u32(sm.raw[ist][1]), &mapL, xs, ys, zs, bar);
-            tma_load_3d(smem_u32(sm.raw[ist][2]), &mapC, xs, ys, zs, bar);
-            prod.advance();
+            tma_load_3d(smem_u32(sm.raw[ist][0]), mS, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][1]), mL, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][2]), mC, xs, ys, zs, bar);
+            if (++p_pz > p_it.z1) {
+                p_item += gridDim.x;
+                p_set();
+            }
             ist = ist + 1 == S ? 0 : ist + 1;
             ++issued;
         };
         if (tid == 0)
-            for (int l = 0; l < S - 2 && prod.valid(); ++l) issue();
+            for (int l = 0; l < S - 2 && p_item < nitems; ++l) issue();
 
         // three register planes whose roles rotate: q-1, q, q+1
         constexpr int H = CY / 2;
@@ -371,15 +402,22 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             RB.S[i] = RB.L[i] = RB.mu[i] = RB.M[i] = RB.c[i] = RB.d[i] = splat(T(0));
         }
 
-        ItemWalk cons;
-        cons.start(blockIdx.x, gridDim.x, nitems, ntiles, zc, g.nz);
         int st = 0, mb = 0, consumed = 0;            // stage / mu-M buffer / count of the current load
         uint32_t par = 0;
         int st_prev = 0, mb_prev = 0;
         bool dead = false;
-        while (cons.valid() && !dead) {
-            const int bx = cons.tile % ntx, by = cons.tile / ntx;
-            const int x0 = bx * TX, y0 = by * TY, z0 = cons.z0, z1 = cons.z1;
+        for (int item = blockIdx.x; item < nitems && !dead; item += gridDim.x) {
+            const Item it = item_at<MULTI>(item, ntiles1, zc1, g1.nz, table, ndom);
+            const Geom g = MULTI ? table[it.dom].g : g1;
+            Fields<T> out = out1;
+            if (MULTI) {
+                out.eS = (T *)table[it.dom].fld[1 - parity][0];
+                out.eL = (T *)table[it.dom].fld[1 - parity][1];
+                out.c = (T *)table[it.dom].fld[1 - parity][2];
+            }
+            const int ntx = MULTI ? table[it.dom].ntx : ntx1;
+            const int bx = it.tile % ntx, by = it.tile / ntx;
+            const int x0 = bx * TX, y0 = by * TY, z0 = it.z0, z1 = it.z1;
             const int X = x0 + tx;
             // per own row j: inside the domain (bit j of vmask), on an x or y face (bit j of emask)
             unsigned vmask = 0, emask = 0;
@@ -431,7 +469,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 }
                 __syncthreads();
                 if (sm.abort) { dead = true; return false; }
-                if (tid == 0 && prod.valid()) issue();   // refill the stage freed two planes ago
+                if (tid == 0 && p_item < nitems) issue();   // refill the stage freed two planes ago
 
                 const int q = pz - 1;
                 if (q >= z0) {
@@ -565,7 +603,26 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     RB = RC;
                 }
             }
-            if (!dead) cons.next_item();
+            if (MULTI && STATS && !dead) {
+                // ensemble: the increment sums of each work item (its domain's)
+                __shared__ double ired[TmaGeo<T>::NT / 32][3];
+                __syncthreads();
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    double v = acc[i];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0) ired[warp][i] = v;
+                    acc[i] = 0.0;
+                }
+                __syncthreads();
+                if (tid == 0)
+                    for (int i = 0; i < 3; ++i) {
+                        double sv = 0;
+                        for (int w = 0; w < TmaGeo<T>::NT / 32; ++w) sv += ired[w][i];
+                        partials[(int64_t)item * 3 + i] = sv;
+                    }
+            }
         }
         if (dead) {
             // drain this CTA's own copies still in flight (bounded), then leave
@@ -575,7 +632,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             return;
         }
     }
-    if (STATS) {
+    if (STATS && !MULTI) {
         // block sum -> partials[blockIdx.x * 3 + i]
         __shared__ double red[TmaGeo<T>::NT / 32][3];
 #pragma unroll
@@ -629,7 +686,10 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map) {
 
 template <typename T, bool ST, bool CO, bool EQ, int R>
 static cudaError_t set_attr1() {
-    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma_smem_bytes<T>());
+    if (e) return e;
+    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)tma_smem_bytes<T>());
 }
 
@@ -666,7 +726,7 @@ int tma_grid(const Geom &g, int num_sms, int *zc_out) {
     if (!occ) {
         if (set_attrs<T>() != cudaSuccess) return -1;
         int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 3>, G::NT,
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 3, false>, G::NT,
                                                           tma_smem_bytes<T>()) != cudaSuccess || o < 1)
             o = 1;
         occ = o;
@@ -709,7 +769,7 @@ int tma_grid_for_zc(const Geom &g, int num_sms, int zc) {
     int dummy = 0;
     if (tma_grid<T>(g, num_sms, &dummy) < 1) return -1;    // attributes + occupancy
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 3>, G::NT,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 3, false>, G::NT,
                                                       tma_smem_bytes<T>()) != cudaSuccess || occ < 1)
         occ = 1;
     const int64_t ntiles = (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY);
@@ -730,8 +790,9 @@ static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, F
     const size_t sh = tma_smem_bytes<T>();
     const bool st = partials != nullptr;
 #define PPF_LAUNCH(ST, CO, EQ)                                                                                      \
-    step_tma_kernel<T, ST, CO, EQ, R><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty, zc, \
-                                                              partials, err, limit_ns, inject_stall)
+    step_tma_kernel<T, ST, CO, EQ, R, false><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty,  \
+                                                                     zc, partials, err, limit_ns, inject_stall,     \
+                                                                     nullptr, 0, 0, 0)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -753,6 +814,70 @@ cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *
     return cudaGetLastError();
 }
 
+template <typename T, int R>
+static void launch_multi_r(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
+                           int parity, double *partials, int grid, int *err, unsigned long long limit_ns,
+                           cudaStream_t s) {
+    using G = TmaGeo<T>;
+    const size_t sh = tma_smem_bytes<T>();
+    const bool st = partials != nullptr;
+    CUtensorMap none;
+    memset(&none, 0, sizeof none);
+    Geom g0;
+    memset(&g0, 0, sizeof g0);
+    const Fields<T> o0 = {nullptr, nullptr, nullptr};
+#define PPF_LAUNCH(ST, CO, EQ)                                                                                 \
+    step_tma_kernel<T, ST, CO, EQ, R, true><<<grid, G::NT, sh, s>>>(none, none, none, g0, k, o0, 1, 1, 1, partials, \
+                                                                    err, limit_ns, 0, table, ndom, items, parity)
+    if (eqA) {
+        if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
+        else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
+    } else {
+        if (!c_only) { if (st) PPF_LAUNCH(true, false, false); else PPF_LAUNCH(false, false, false); }
+        else { if (st) PPF_LAUNCH(true, true, false); else PPF_LAUNCH(false, true, false); }
+    }
+#undef PPF_LAUNCH
+}
+
+template <typename T>
+cudaError_t launch_step_multi(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
+                              int parity, double *partials, int grid, int roll, int *err,
+                              unsigned long long limit_ns, cudaStream_t s) {
+    if (roll == 1) launch_multi_r<T, 1>(table, ndom, items, k, c_only, eqA, parity, partials, grid, err, limit_ns, s);
+    else launch_multi_r<T, 3>(table, ndom, items, k, c_only, eqA, parity, partials, grid, err, limit_ns, s);
+    return cudaGetLastError();
+}
+
+template <typename T>
+void step_tile(int *tx, int *ty) {
+    *tx = TmaGeo<T>::TX;
+    *ty = TmaGeo<T>::TY;
+}
+
+template <typename T>
+int tma_grid_items(int64_t items, int num_sms) {
+    Geom g;
+    memset(&g, 0, sizeof g);
+    g.nx = g.ny = g.nz = 1;
+    int zc = 1;
+    if (tma_grid<T>(g, num_sms, &zc) < 1) return -1;     // attributes + occupancy
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 3, true>,
+                                                      TmaGeo<T>::NT, tma_smem_bytes<T>()) != cudaSuccess ||
+        occ < 1)
+        occ = 1;
+    const int64_t slots = (int64_t)occ * num_sms;
+    return (int)(items < slots ? items : slots);
+}
+
+template void step_tile<float>(int *, int *);
+template void step_tile<double>(int *, int *);
+template int tma_grid_items<float>(int64_t, int);
+template int tma_grid_items<double>(int64_t, int);
+template cudaError_t launch_step_multi<float>(const DomainDesc *, int, int, const Coef<float> &, bool, bool, int,
+                                              double *, int, int, int *, unsigned long long, cudaStream_t);
+template cudaError_t launch_step_multi<double>(const DomainDesc *, int, int, const Coef<double> &, bool, bool, int,
+                                               double *, int, int, int *, unsigned long long, cudaStream_t);
 template int make_field_map<float>(const Geom &, const float *, CUtensorMap *);
 template int make_field_map<double>(const Geom &, const double *, CUtensorMap *);
 template int tma_grid<float>(const Geom &, int, int *);

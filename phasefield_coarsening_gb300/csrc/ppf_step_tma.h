@@ -8,6 +8,17 @@
 
 namespace ppf {
 
+// One domain of an ensemble, as the fused step reads it from device memory
+// (the TMA descriptors are used from there directly).
+struct alignas(128) DomainDesc {
+    CUtensorMap maps[2][3];   // [buffer][etaS, etaL, c]
+    Geom g;
+    void *fld[2][3];          // [buffer][etaS, etaL, c]
+    int ntx, nty;             // tiles in x and y
+    int zc, nc;               // z planes per work item, items per tile column
+    int item0, nitems;        // first work item of this domain in the ensemble, count
+};
+
 // Launch choices of the fused step that the autotuner may change.
 struct StepTune {
     int grid;   // persistent CTAs
@@ -38,5 +49,21 @@ template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
                             bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
                             int inject_stall, cudaStream_t s);
+
+// Tiles of the fused step (x, y), for sizing ensemble work items.
+template <typename T>
+void step_tile(int *tx, int *ty);
+
+// Persistent grid for `items` work items (occupancy x SMs, capped).
+template <typename T>
+int tma_grid_items(int64_t items, int num_sms);
+
+// One fused step of every domain of an ensemble: reads buffer `parity` of
+// each domain and writes buffer 1-parity.  `partials` (nullable) receives 3
+// doubles per work item (the last-step increment sums).
+template <typename T>
+cudaError_t launch_step_multi(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
+                              int parity, double *partials, int grid, int roll, int *err,
+                              unsigned long long limit_ns, cudaStream_t s);
 
 }  // namespace ppf

@@ -175,6 +175,29 @@ def workload(name: str, seed: int = 0, shape=None):
     return generate(w["shape"], radius=w["radius"], count=w["count"], vf=w["vf"], seed=seed)
 
 
+def ensemble_workload(n=64, edges=(48, 64, 96, 128), vf=(0.1, 0.4), radius=("lognormal", 5.0, 0.3), seed=0):
+    """Ensemble of `n` cubic periodic domains: edge drawn from `edges`,
+    target solid fraction from U[vf], lognormal radii, each domain with its
+    own seed.  Targets above what random non-overlapping placement reaches
+    (about 0.34 with a one-cell gap) are placed with touching allowed
+    (gap 0); spheres that find no place are dropped, so the achieved
+    fraction ("sphere_fraction" in each info) can fall below the target.
+    Returns a list of (etaS, etaL, c, info)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for d in range(n):
+        e = int(rng.choice(edges))
+        f = float(rng.uniform(*vf))
+        shape = (e, e, e)
+        r = np.random.default_rng([seed, d])
+        cen, rad = place_particles(shape, r, radius, vf=f, gap=1.0 if f <= 0.3 else 0.0)
+        etaS, etaL, c = render(shape, cen, rad, rng=r)
+        info = {"edge": e, "target_fraction": f, "particles": int(len(rad)),
+                "sphere_fraction": float((4 / 3 * math.pi * rad ** 3).sum() / np.prod(shape)), "seed": [seed, d]}
+        out.append((etaS, etaL, c, info))
+    return out
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser(description="write a seeded particle microstructure as an HDF5 input for ppf")
     ap.add_argument("out")

@@ -247,6 +247,58 @@ int ppf_ensemble_set_tune(ppf_ensemble *ens, const ppf_tune *t);
 /* Like ppf_autotune, over the whole ensemble (states kept). */
 int ppf_ensemble_autotune(ppf_ensemble *ens, int trial_steps, ppf_tune *best);
 
+/* Solute-mass projection of an FP32 state: sum(c) over the interior is set
+ * to target_mass (FP64 arithmetic; the deficit is spread over the cells in
+ * whole FP32 ulps, so the FP32 sum lands within about one ulp of it).  The
+ * reference conserves mass in FP64 arithmetic alone (phasefield.c:374-384,
+ * summed at :228-238); FP32 storage needs the projection for drift below
+ * 1e-9 relative over long runs. */
+int ppf_mass_project(ppf_ctx *ctx, double target_mass);
+
+/* dst's state := src's current state (same shape, precision and BC). */
+int ppf_copy_state(ppf_ctx *dst, ppf_ctx *src);
+
+/* Learned time-stepping surrogate (no counterpart in the reference): a
+ * six-layer 3x3x3 convolutional network, BF16 tensor-core implicit GEMMs
+ * with FP32 accumulation, that advances an FP32 state by k_steps explicit
+ * steps of sweep_fields (phasefield.c:301-403) per call:
+ *   state += out_scale * net(etaS, etaL, (c - c_eq(h)) * in_scale_c)
+ * followed by the FP64 mass projection back to the pre-call sum(c).
+ * Trained on the device on (state, state after k_steps stencil steps)
+ * pairs.  Domains: FP32 contexts whose x edge is a multiple of 128;
+ * training on periodic domains. */
+typedef struct ppf_surrogate ppf_surrogate;
+
+typedef struct {
+    int width;              /* hidden channels: 16 or 32 */
+    int k_steps;            /* explicit steps one call stands for */
+    double c_solid;         /* c_eq(h) = h c_solid + (1 - h) c_liquid */
+    double c_liquid;
+    double in_scale_c;      /* scale of the composition feature */
+    double out_scale[3];    /* field change per unit of network output: etaS, etaL, c */
+    double loss_weight[3];  /* per-field weights of the squared-error loss */
+} ppf_surrogate_config;
+
+void ppf_surrogate_config_default(ppf_surrogate_config *cfg);
+int ppf_surrogate_create(const ppf_surrogate_config *cfg, ppf_surrogate **out);
+int ppf_surrogate_destroy(ppf_surrogate *s);
+int ppf_surrogate_get_config(const ppf_surrogate *s, ppf_surrogate_config *cfg);
+/* Parameters: per layer W[27][c_out][c_in] (tap = (dz+1)*9 + (dy+1)*3 + (dx+1),
+ * out[v] = sum W_tap in[v + (dx,dy,dz)]) then b[c_out]; channels 16, width x5, 16. */
+int64_t ppf_surrogate_num_params(const ppf_surrogate *s);
+int ppf_surrogate_set_params(ppf_surrogate *s, const float *params, int64_t n);
+int ppf_surrogate_get_params(ppf_surrogate *s, float *params, int64_t n);
+/* Loss = sum over cells and fields of loss_weight (pred - (target - input) / out_scale)^2 / (3 cells),
+ * and its gradient (grad may be NULL); no update. */
+int ppf_surrogate_loss_grad(ppf_surrogate *s, ppf_ctx *input, ppf_ctx *target, double *loss, float *grad,
+                            int64_t n);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on one (input, target) pair; loss may be NULL. */
+int ppf_surrogate_train_step(ppf_surrogate *s, ppf_ctx *input, ppf_ctx *target, double lr, double *loss);
+/* Predicted change out_scale * net(.) of etaS, etaL, c: 3 x cells doubles, [field][z][y][x]. */
+int ppf_surrogate_predict(ppf_surrogate *s, ppf_ctx *ctx, double *out3);
+/* ncalls surrogate calls on ctx's state (k_steps each, mass projected after each). */
+int ppf_surrogate_advance(ppf_surrogate *s, ppf_ctx *ctx, int ncalls);
+
 /* Message for the calling thread's last failure ("" if none). */
 const char *ppf_last_error(void);
 

@@ -31,7 +31,10 @@ EXPORTS = (
     "ppf_autotune", "ppf_observe_noalloc", "ppf_particles", "ppf_ensemble_create", "ppf_ensemble_destroy",
     "ppf_ensemble_domain", "ppf_ensemble_upload", "ppf_ensemble_download", "ppf_ensemble_step",
     "ppf_ensemble_reduce", "ppf_ensemble_sync", "ppf_ensemble_get_tune", "ppf_ensemble_set_tune",
-    "ppf_ensemble_autotune", "ppf_last_error", "ppf_version",
+    "ppf_ensemble_autotune", "ppf_mass_project", "ppf_copy_state", "ppf_surrogate_config_default",
+    "ppf_surrogate_create", "ppf_surrogate_destroy", "ppf_surrogate_get_config", "ppf_surrogate_num_params",
+    "ppf_surrogate_set_params", "ppf_surrogate_get_params", "ppf_surrogate_loss_grad", "ppf_surrogate_train_step",
+    "ppf_surrogate_predict", "ppf_surrogate_advance", "ppf_last_error", "ppf_version",
     "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_last_error",
 )
 
@@ -78,6 +81,17 @@ class ParticleStats(ctypes.Structure):
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class SurrogateConfig(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int), ("k_steps", ctypes.c_int), ("c_solid", ctypes.c_double),
+                ("c_liquid", ctypes.c_double), ("in_scale_c", ctypes.c_double),
+                ("out_scale", ctypes.c_double * 3), ("loss_weight", ctypes.c_double * 3)]
+
+    def as_dict(self) -> dict:
+        return {"width": self.width, "k_steps": self.k_steps, "c_solid": self.c_solid, "c_liquid": self.c_liquid,
+                "in_scale_c": self.in_scale_c, "out_scale": list(self.out_scale),
+                "loss_weight": list(self.loss_weight)}
 
 
 class PPFError(RuntimeError):
@@ -131,6 +145,23 @@ def lib() -> ctypes.CDLL:
         L.ppf_ensemble_get_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
         L.ppf_ensemble_set_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
         L.ppf_ensemble_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Tune)]
+        L.ppf_mass_project.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.ppf_copy_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.ppf_surrogate_config_default.argtypes = [ctypes.POINTER(SurrogateConfig)]
+        L.ppf_surrogate_config_default.restype = None
+        L.ppf_surrogate_create.argtypes = [ctypes.POINTER(SurrogateConfig), ctypes.POINTER(ctypes.c_void_p)]
+        L.ppf_surrogate_destroy.argtypes = [ctypes.c_void_p]
+        L.ppf_surrogate_get_config.argtypes = [ctypes.c_void_p, ctypes.POINTER(SurrogateConfig)]
+        L.ppf_surrogate_num_params.argtypes = [ctypes.c_void_p]
+        L.ppf_surrogate_num_params.restype = ctypes.c_int64
+        for n in ("ppf_surrogate_set_params", "ppf_surrogate_get_params"):
+            getattr(L, n).argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+        L.ppf_surrogate_loss_grad.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.POINTER(ctypes.c_double), ctypes.c_void_p, ctypes.c_int64]
+        L.ppf_surrogate_train_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                                               ctypes.POINTER(ctypes.c_double)]
+        L.ppf_surrogate_predict.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.ppf_surrogate_advance.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.ppf_h5_dims.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.ppf_h5_read3d.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _dp,
                                     ctypes.c_int64]
@@ -270,6 +301,87 @@ class Simulation:
         s = Stats()
         _check(lib().ppf_reduce(self._h, ctypes.byref(s)))
         return s.as_dict()
+
+    def mass_project(self, target_mass: float):
+        """Set sum(c) to target_mass (FP32 states; FP64 arithmetic)."""
+        _check(lib().ppf_mass_project(self._h, float(target_mass)))
+
+    def copy_from(self, other: "Simulation"):
+        """This state := other's current state (same shape, precision, BC)."""
+        _check(lib().ppf_copy_state(self._h, other._h))
+
+
+class Surrogate:
+    """Host-side mirror of a ppf_surrogate: the learned k-step network
+    (six 3x3x3 convolutions, BF16 tensor-core kernels), its training on the
+    device, and its use as a time stepper with FP64 mass projection."""
+
+    def __init__(self, width: int = 32, k_steps: int = 50, **overrides):
+        cfg = SurrogateConfig()
+        lib().ppf_surrogate_config_default(ctypes.byref(cfg))
+        cfg.width = int(width)
+        cfg.k_steps = int(k_steps)
+        for k, v in overrides.items():
+            if k in ("out_scale", "loss_weight"):
+                setattr(cfg, k, (ctypes.c_double * 3)(*[float(x) for x in v]))
+            else:
+                setattr(cfg, k, v)
+        h = ctypes.c_void_p()
+        _check(lib().ppf_surrogate_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ppf_surrogate_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def config(self) -> dict:
+        c = SurrogateConfig()
+        _check(lib().ppf_surrogate_get_config(self._h, ctypes.byref(c)))
+        return c.as_dict()
+
+    @property
+    def num_params(self) -> int:
+        return int(lib().ppf_surrogate_num_params(self._h))
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params, np.float32)
+        _check(lib().ppf_surrogate_get_params(self._h, out.ctypes.data, out.size))
+        return out
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        _check(lib().ppf_surrogate_set_params(self._h, p.ctypes.data, p.size))
+
+    def loss_grad(self, inp: Simulation, tgt: Simulation):
+        g = np.empty(self.num_params, np.float32)
+        loss = ctypes.c_double()
+        _check(lib().ppf_surrogate_loss_grad(self._h, inp._h, tgt._h, ctypes.byref(loss), g.ctypes.data, g.size))
+        return loss.value, g
+
+    def train_step(self, inp: Simulation, tgt: Simulation, lr: float = 1e-3, want_loss: bool = True):
+        loss = ctypes.c_double()
+        _check(lib().ppf_surrogate_train_step(self._h, inp._h, tgt._h, float(lr),
+                                              ctypes.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def predict(self, sim: Simulation):
+        """Predicted change of (etaS, etaL, c) over k_steps (float64, [z][y][x] each)."""
+        out = np.empty((3,) + tuple(sim.shape), np.float64)
+        _check(lib().ppf_surrogate_predict(self._h, sim._h, out.ctypes.data))
+        return out
+
+    def advance(self, sim: Simulation, ncalls: int = 1):
+        _check(lib().ppf_surrogate_advance(self._h, sim._h, int(ncalls)))
 
 
 class Ensemble:

@@ -58,7 +58,7 @@ enum Epi : int {
 struct ConvArgs {
     NNGeom g;
     const uint16_t *x;      // input, CI channels (planar padded)
-    const uint16_t *wimg;   // weight image: [27][CI/8][CO][8] BF16
+    const uint16_t *wimg;   // weight image: [dz][dx][CI/8][dy][CO][8] BF16
     const float *bias;      // CO
     uint16_t *out;          // output, CO channels (planar padded)
     uint16_t *zout;         // pre-activations (EPI_ACT_TRAIN), interior only
@@ -86,6 +86,7 @@ struct WgradArgs {
 };
 
 int conv_smem_bytes(int ci, int co);
+int conv_ctas_per_sm(int ci, int co);
 int wgrad_smem_bytes(int cx, int cz);
 cudaError_t conv_setup(int max_smem_optin);
 cudaError_t launch_conv(int ci, int co, int epi, const ConvArgs &a, int grid, cudaStream_t s);

@@ -125,19 +125,23 @@ constexpr int kConvThreads = 320;   // producer warp, MMA warp, 8 epilogue warps
 
 template <int CI, int CO>
 struct ConvCfg {
-    static constexpr int RING = 5;                       // row slots
+    static constexpr int RING = CI == 32 ? 6 : 5;        // input-row slots in shared memory
+    static constexpr int ND = 5;                         // TMEM tiles (one per input row)
+    static constexpr int NCOL = 3 * CO;                  // one tile: contributions to rows y+1, y, y-1
     static constexpr int SEGB = (CI / 8) * kSegPlane;    // one segment, all channel planes
     static constexpr int ROWB = 3 * SEGB;                // one slot: segments at z-1, z, z+1
     static constexpr int WB = 27 * CI * CO * 2;          // weight image
-    static constexpr int HALF = CO / 2;                  // TMEM columns per epilogue warp
+    static constexpr int HALF = CO / 2;                  // output channels per epilogue warp
     static constexpr int OFF_W = RING * ROWB;
     static constexpr int OFF_BAR = OFF_W + WB;
-    static constexpr int NBAR = 2 * RING + 6;            // full, empty, accfull[2], accempty[2], wbar, drain
+    static constexpr int NBAR = 2 * RING + 2 * ND + 2;   // full, empty, dfull, dempty, wbar, drain
     static constexpr int OFF_SLOT = OFF_BAR + NBAR * 8;  // TMEM base, abort flag
     static constexpr int OFF_RED = OFF_SLOT + 16;        // [8][HALF + 1] floats
-    static constexpr int SMEM = OFF_RED + 8 * (HALF + 1) * 4;
-    static constexpr int TMEM_COLS = 2 * CO < 32 ? 32 : 2 * CO;
+    static constexpr int OFF_BIAS = OFF_RED + 8 * (HALF + 1) * 4;   // CO floats
+    static constexpr int SMEM = OFF_BIAS + CO * 4;
+    static constexpr int TMEM_COLS = ND * NCOL <= 256 ? 256 : 512;
     static_assert(CI % 16 == 0 && CO % 16 == 0 && CO <= 32, "channel counts");
+    static_assert(ND * NCOL <= 512 && NCOL <= 256, "TMEM / MMA N");
     static_assert(OFF_W % 16 == 0 && OFF_BAR % 8 == 0, "alignment");
 };
 
@@ -159,6 +163,13 @@ __device__ __forceinline__ Item item_of(const NNGeom &g, int yc, int it) {
     return r;
 }
 
+// Work order inside a CTA: items in turn, and in an item the input rows
+// y0-1 .. y1 in order; input row number q (counted over the CTA's items)
+// owns shared-memory slot q % RING and TMEM tile q % ND.  The MMAs of row q
+// compute, for the 128 voxels of the tile and all three dy at once
+// (N = 3 CO), D_q[v][(dy, co)] = sum over (dz, dx, ci) of
+// W[dz][dy][dx][co][ci] in[z+dz][row q][x+dx][ci]; output row y is
+// D_{y-1}[dy=-1] + D_y[dy=0] + D_{y+1}[dy=+1], summed by the epilogue.
 template <int CI, int CO, int EPI>
 __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a) {
     using C = ConvCfg<CI, CO>;
@@ -167,24 +178,26 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t sb = smem_u32(smem);
     const uint32_t ring = sb, wsm = sb + C::OFF_W, bars = sb + C::OFF_BAR;
-    const uint32_t wbar = bars + 8 * (2 * C::RING + 4), dbar = wbar + 8;
+    const uint32_t wbar = bars + 8 * (2 * C::RING + 2 * C::ND), dbar = wbar + 8;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + C::OFF_SLOT);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + C::OFF_SLOT + 4);
     float *red = reinterpret_cast<float *>(smem + C::OFF_RED);
+    float *sbias = reinterpret_cast<float *>(smem + C::OFF_BIAS);
     auto full = [&](uint32_t s) { return bars + 8 * s; };
     auto empty = [&](uint32_t s) { return bars + 8 * (C::RING + s); };
-    auto accfull = [&](uint32_t s) { return bars + 8 * (2 * C::RING + s); };
-    auto accempty = [&](uint32_t s) { return bars + 8 * (2 * C::RING + 2 + s); };
+    auto dfull = [&](uint32_t s) { return bars + 8 * (2 * C::RING + s); };
+    auto dempty = [&](uint32_t s) { return bars + 8 * (2 * C::RING + C::ND + s); };
     const NNGeom &g = a.g;
 
+    if (tid < CO) sbias[tid] = a.bias[tid];
     if (tid == 0) {
         for (int s = 0; s < C::RING; ++s) {
             mbar_init(full(s), 1);
             mbar_init(empty(s), 1);
         }
-        for (int s = 0; s < 2; ++s) {
-            mbar_init(accfull(s), 1);
-            mbar_init(accempty(s), kConvThreads - 64);
+        for (int s = 0; s < C::ND; ++s) {
+            mbar_init(dfull(s), 1);
+            mbar_init(dempty(s), kConvThreads - 64);
         }
         mbar_init(wbar, 1);
         mbar_init(dbar, 1);
@@ -241,62 +254,45 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
             if (!mbar_wait(wbar, 0, a.limit_ns)) atomicOr(a.err, 4);
         }
     } else if (warp == 1) {
-        // ---------------- MMA issuer ----------------
+        // ---------------- MMA issuer: one D tile per input row ----------------
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(128, CO, false, false);
+            const uint32_t idesc = idesc_bf16(128, C::NCOL, false, false);
             // descriptors of slot 0 and of the weight image; every operand
             // below is one of these plus a byte offset / 16 (no carry: all
-            // shared addresses stay below 2^18)
+            // shared addresses stay below 2^18).  Weight image rows for
+            // (dz, dx, 8-channel group j) are (dy, co): N = 3 CO rows.
             const uint64_t a0 = smem_desc(ring, kSegPlane, 128);
-            const uint64_t b0 = smem_desc(wsm, CO * 16, 128);
+            const uint64_t b0 = smem_desc(wsm, C::NCOL * 16, 128);
             bool ok = wait_or_abort(wbar, 0, a.limit_ns, abort_flag);
             if (!ok) fail(abort_flag, a.err, 1);
-            uint32_t q = 0, t = 0;
+            uint32_t q = 0;
             for (int it = blockIdx.x; ok && it < a.items; it += gridDim.x) {
                 const Item w = item_of(g, a.yc, it);
-                const uint32_t qb = q;   // sequence number of row y0 - 1
-                for (int y = w.y0; ok && y < w.y1; ++y) {
-                    const uint32_t qr = qb + (uint32_t)(y - w.y0);   // row y - 1
-                    for (uint32_t k = (y == w.y0 ? 0u : 2u); k < 3u; ++k) {
-                        const uint32_t qq = qr + k;
-                        if (!wait_or_abort(full(qq % C::RING), (qq / C::RING) & 1, a.limit_ns, abort_flag)) {
-                            ok = false;
-                            break;
-                        }
-                    }
-                    const uint32_t acc = t & 1;
-                    if (ok && !wait_or_abort(accempty(acc), ((t >> 1) + 1) & 1, a.limit_ns, abort_flag)) ok = false;
-                    if (!ok) {
+                for (int r = w.y0 - 1; r <= w.y1; ++r, ++q) {
+                    const uint32_t s = q % C::RING, ds = q % C::ND;
+                    if (!wait_or_abort(full(s), (q / C::RING) & 1, a.limit_ns, abort_flag) ||
+                        (q >= (uint32_t)C::ND &&
+                         !wait_or_abort(dempty(ds), ((q / C::ND) + 1) & 1, a.limit_ns, abort_flag))) {
                         fail(abort_flag, a.err, 1);
+                        ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t d = tbase + acc * CO;
-                    uint64_t ab[3];
-#pragma unroll
-                    for (int dy = 0; dy < 3; ++dy) ab[dy] = a0 + ((((qr + dy) % C::RING) * C::ROWB) >> 4);
+                    const uint32_t d = tbase + ds * C::NCOL;
+                    const uint64_t ab = a0 + ((s * C::ROWB) >> 4);
 #pragma unroll
                     for (int dz = 0; dz < 3; ++dz)
 #pragma unroll
-                        for (int dy = 0; dy < 3; ++dy)
+                        for (int dx = 0; dx < 3; ++dx)
 #pragma unroll
-                            for (int dx = 0; dx < 3; ++dx)
-#pragma unroll
-                                for (int kk = 0; kk < CI / 16; ++kk) {
-                                    const int tap = dz * 9 + dy * 3 + dx;
-                                    const uint64_t ad = ab[dy] + ((dz * C::SEGB + dx * 16 + kk * 2 * kSegPlane) >> 4);
-                                    const uint64_t bd = b0 + ((tap * CI * CO * 2 + kk * 2 * CO * 16) >> 4);
-                                    mma_bf16(d, ad, bd, idesc, (tap | kk) ? 1u : 0u);
-                                }
-                    mma_commit(accfull(acc));
-                    mma_commit(empty(qr % C::RING));
-                    if (y == w.y1 - 1) {
-                        mma_commit(empty((qr + 1) % C::RING));
-                        mma_commit(empty((qr + 2) % C::RING));
-                    }
-                    ++t;
+                            for (int kk = 0; kk < CI / 16; ++kk) {
+                                const uint64_t ad = ab + ((dz * C::SEGB + dx * 16 + kk * 2 * kSegPlane) >> 4);
+                                const uint64_t bd = b0 + ((((dz * 3 + dx) * (CI / 8) + 2 * kk) * C::NCOL * 16) >> 4);
+                                mma_bf16(d, ad, bd, idesc, (dz | dx | kk) ? 1u : 0u);
+                            }
+                    mma_commit(empty(s));
+                    mma_commit(dfull(ds));
                 }
-                q = qb + (uint32_t)(w.y1 - w.y0) + 2;
             }
             // drain: all issued MMAs complete before TMEM is released
             mma_commit(dbar);
@@ -304,24 +300,28 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
         }
     } else {
         // ---------------- epilogue: 8 warps; TMEM lane quarter = warp % 4,
-        // columns [c0, c0 + HALF) by warp group ----------------
+        // output channels [c0, c0 + HALF) by warp group ----------------
         const int ew = warp - 2;
         const int quarter = warp & 3;
         const int c0 = (ew >> 2) * HALF;
         const int row = quarter * 32 + lane;
+        const uint32_t tl = tbase + ((uint32_t)(quarter * 32) << 16) + c0;
         constexpr bool STATE_OUT = EPI == EPI_STATE || EPI == EPI_LOSS;
         const bool active = !STATE_OUT || c0 == 0;
         float sums[HALF + 1];
 #pragma unroll
         for (int c = 0; c <= HALF; ++c) sums[c] = 0.f;
-        uint32_t t = 0;
+        uint32_t q = 0;
         bool ok = true;
         for (int it = blockIdx.x; ok && it < a.items; it += gridDim.x) {
             const Item w = item_of(g, a.yc, it);
-            for (int y = w.y0; y < w.y1; ++y, ++t) {
+            const uint32_t qb = q;                 // input row y0 - 1
+            q += (uint32_t)(w.y1 - w.y0) + 2;
+            for (int y = w.y0; y < w.y1; ++y) {
+                const uint32_t qy = qb + (uint32_t)(y - w.y0) + 1;   // input row y
                 const int x = w.x0 + row, z = w.z;
                 const int64_t p = g.p(x, y, z);
-                // loads that do not depend on the accumulator go first
+                // loads that do not depend on the accumulators go first
                 float zl[HALF];
                 float s0v[3] = {0.f, 0.f, 0.f}, s1v[3] = {0.f, 0.f, 0.f};
                 int64_t sa = 0;
@@ -343,8 +343,9 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                         s1v[2] = a.s1.c[sa];
                     }
                 }
-                const uint32_t acc = t & 1;
-                if (!wait_or_abort(accfull(acc), (t >> 1) & 1, a.limit_ns, abort_flag)) {
+                if (!wait_or_abort(dfull((qy - 1) % C::ND), ((qy - 1) / C::ND) & 1, a.limit_ns, abort_flag) ||
+                    !wait_or_abort(dfull(qy % C::ND), (qy / C::ND) & 1, a.limit_ns, abort_flag) ||
+                    !wait_or_abort(dfull((qy + 1) % C::ND), ((qy + 1) / C::ND) & 1, a.limit_ns, abort_flag)) {
                     fail(abort_flag, a.err, 1);
                     ok = false;
                     break;
@@ -352,21 +353,33 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                 tc_fence_after();
                 float v[HALF];
                 {
-                    const uint32_t ta = tbase + ((uint32_t)(quarter * 32) << 16) + acc * CO + c0;
+                    // out[y] = sum_dy W_dy in[y + dy]: the dy = -1 block of
+                    // D_{y-1}, the dy = 0 block of D_y, the dy = +1 block of D_{y+1}
+                    const uint32_t t0 = tl + ((qy - 1) % C::ND) * C::NCOL;
+                    const uint32_t t1 = tl + (qy % C::ND) * C::NCOL + CO;
+                    const uint32_t t2 = tl + ((qy + 1) % C::ND) * C::NCOL + 2 * CO;
                     if constexpr (HALF == 16) {
-                        float tmp[16];
-                        tmem_ld16(ta, tmp);
+                        float u0[16], u1[16], u2[16];
+                        tmem_ld16(t0, u0);
+                        tmem_ld16(t1, u1);
+                        tmem_ld16(t2, u2);
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) v[i] = tmp[i];
+                        for (int i = 0; i < 16; ++i) v[i] = (u0[i] + u1[i]) + u2[i];
                     } else {
-                        float tmp[8];
-                        tmem_ld8(ta, tmp);
+                        float u0[8], u1[8], u2[8];
+                        tmem_ld8(t0, u0);
+                        tmem_ld8(t1, u1);
+                        tmem_ld8(t2, u2);
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) v[i] = tmp[i];
+                        for (int i = 0; i < 8; ++i) v[i] = (u0[i] + u1[i]) + u2[i];
                     }
                 }
                 tc_fence_before();
-                mbar_arrive(accempty(acc));
+                mbar_arrive(dempty((qy - 1) % C::ND));
+                if (y == w.y1 - 1) {
+                    mbar_arrive(dempty(qy % C::ND));
+                    mbar_arrive(dempty((qy + 1) % C::ND));
+                }
 
                 if (EPI == EPI_ACT || EPI == EPI_ACT_TRAIN) {
                     uint4 o[HALF / 8], zz[HALF / 8];
@@ -375,7 +388,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                         float h[8], sv[8];
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
-                            h[i] = v[8 * j + i] + __ldg(a.bias + c0 + 8 * j + i);
+                            h[i] = v[8 * j + i] + sbias[c0 + 8 * j + i];
                             sv[i] = h[i] * sigmoidf(h[i]);
                         }
                         o[j] = pack8(sv);
@@ -393,15 +406,15 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                     uint4 o[HALF / 8];
 #pragma unroll
                     for (int j = 0; j < HALF / 8; ++j) {
-                        float d[8];
+                        float dd[8];
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
                             const float zi = zl[8 * j + i];
                             const float sg = sigmoidf(zi);
-                            d[i] = v[8 * j + i] * sg * (1.0f + zi * (1.0f - sg));
-                            sums[8 * j + i] += d[i];
+                            dd[i] = v[8 * j + i] * sg * (1.0f + zi * (1.0f - sg));
+                            sums[8 * j + i] += dd[i];
                         }
-                        o[j] = pack8(d);
+                        o[j] = pack8(dd);
                     }
                     uint16_t *ob = reinterpret_cast<uint16_t *>(reinterpret_cast<unsigned char *>(a.out) +
                                                                 (int64_t)(c0 / 8) * g.Pst * 16);
@@ -411,7 +424,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                         const Geom &sg = a.sg;
                         float nv[3];
 #pragma unroll
-                        for (int k = 0; k < 3; ++k) nv[k] = s0v[k] + a.oscale[k] * (v[k] + __ldg(a.bias + k));
+                        for (int k = 0; k < 3; ++k) nv[k] = s0v[k] + a.oscale[k] * (v[k] + sbias[k]);
                         // the stencil's face ghosts: written by the cell they mirror
                         const int ax = image_of(x, sg.nx, sg.bc), ay = image_of(y, sg.ny, sg.bc),
                                   az = image_of(z, sg.nz, sg.bc);
@@ -437,7 +450,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
 #pragma unroll
                         for (int c = 0; c < 3; ++c) {
                             const float tg = (s1v[c] - s0v[c]) / a.oscale[c];
-                            const float diff = v[c] + __ldg(a.bias + c) - tg;
+                            const float diff = v[c] + sbias[c] - tg;
                             sums[HALF] += a.lw[c] * diff * diff;
                             gr[c] = 2.0f * a.lw[c] * diff;
                             sums[c] += gr[c];
@@ -690,6 +703,23 @@ cudaError_t wgrad_attr() {
 }
 
 }  // namespace
+
+template <int CI, int CO>
+int conv_per_sm() {
+    // shared memory (228 KB per SM, 1 KB reserved per CTA) and TMEM (512 columns per SM)
+    const int by_smem = 233472 / (ConvCfg<CI, CO>::SMEM + 1024);
+    const int by_tmem = 512 / ConvCfg<CI, CO>::TMEM_COLS;
+    const int n = by_smem < by_tmem ? by_smem : by_tmem;
+    return n < 1 ? 1 : n;
+}
+
+int conv_ctas_per_sm(int ci, int co) {
+    if (ci == 16 && co == 16) return conv_per_sm<16, 16>();
+    if (ci == 16 && co == 32) return conv_per_sm<16, 32>();
+    if (ci == 32 && co == 16) return conv_per_sm<32, 16>();
+    if (ci == 32 && co == 32) return conv_per_sm<32, 32>();
+    return 1;
+}
 
 int conv_smem_bytes(int ci, int co) {
     if (ci == 16 && co == 16) return ConvCfg<16, 16>::SMEM;

@@ -168,16 +168,20 @@ __global__ void __launch_bounds__(kNT) adam_kernel(int64_t n, float *p, const fl
     }
 }
 
-// W[27][co][ci] (FP32) -> forward image [27][ci/8][co][8] and transposed,
-// tap-reversed image [27][co/8][ci][8] of the input-gradient convolution
+// W[27][co][ci] (FP32, tap = 9 dz + 3 dy + dx over 0..2) -> the BF16
+// B-operand images of the convolution kernel, [dz][dx][ci/8][dy][co][8]
+// (one MMA's N = 3 co rows are the three dy taps), forward and for the
+// input-gradient convolution (taps reversed, ci and co swapped).
 __global__ void __launch_bounds__(kNT) pack_kernel(const float *W, int ci, int co, uint16_t *wf, uint16_t *wb) {
     const int n = 27 * ci * co;
     for (int i = blockIdx.x * kNT + threadIdx.x; i < n; i += gridDim.x * kNT) {
         const int c_in = i % ci, c_out = (i / ci) % co, tap = i / (ci * co);
+        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
         const __nv_bfloat16 h = __float2bfloat16_rn(W[i]);
         const uint16_t u = *reinterpret_cast<const uint16_t *>(&h);
-        wf[(((int64_t)tap * (ci / 8) + c_in / 8) * co + c_out) * 8 + (c_in & 7)] = u;
-        wb[(((int64_t)(26 - tap) * (co / 8) + c_out / 8) * ci + c_in) * 8 + (c_out & 7)] = u;
+        wf[((((int64_t)(dz * 3 + dx) * (ci / 8) + c_in / 8) * 3 + dy) * co + c_out) * 8 + (c_in & 7)] = u;
+        const int rz = 2 - dz, ry = 2 - dy, rx = 2 - dx;
+        wb[((((int64_t)(rz * 3 + rx) * (co / 8) + c_out / 8) * 3 + ry) * ci + c_in) * 8 + (c_out & 7)] = u;
     }
 }
 
@@ -478,13 +482,8 @@ extern "C" int ppf_surrogate_create(const ppf_surrogate_config *cfg, ppf_surroga
         off += s->co[l];
     }
     s->nparams = off;
-    // CTAs per SM from shared memory (1 KB reserved per CTA, 228 KB per SM)
     for (int a = 0; a < 2; ++a)
-        for (int b = 0; b < 2; ++b) {
-            const int sm = conv_smem_bytes(a ? 32 : 16, b ? 32 : 16);
-            const int per = std::max(1, std::min(2, 233472 / (sm + 1024)));
-            s->conv_grid[a][b] = per * s->num_sms;
-        }
+        for (int b = 0; b < 2; ++b) s->conv_grid[a][b] = conv_ctas_per_sm(a ? 32 : 16, b ? 32 : 16) * s->num_sms;
     s->wgrad_grid = s->num_sms;
     const size_t pb = (size_t)s->nparams * sizeof(float);
     bool ok = cudaMalloc(&s->params, pb) == cudaSuccess && cudaMalloc(&s->grads, pb) == cudaSuccess &&

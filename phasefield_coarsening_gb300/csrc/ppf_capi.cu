@@ -170,14 +170,14 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
     cudaError_t e1 = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
     cudaError_t e2 = e1 == cudaSuccess ? cudaMalloc(&c->state, 6 * fbytes) : e1;
     cudaError_t e3 = e2 == cudaSuccess ? cudaMalloc(&c->staging, 3 * (size_t)cells * sizeof(double)) : e2;
-    cudaError_t e4 = e3 == cudaSuccess ? cudaMalloc(&c->dres, 16 * sizeof(double) + 64) : e3;
+    cudaError_t e4 = e3 == cudaSuccess ? cudaMalloc(&c->dres, 32 * sizeof(double) + 64) : e3;
     if (e4 != cudaSuccess) {
         ppf_destroy(c);
         return seterr(e4 == cudaErrorMemoryAllocation ? PPF_ENOMEM : PPF_ECUDA, "device setup failed: %s",
                       cudaGetErrorString(e4));
     }
     c->stream = c->own;
-    c->derr = (int *)(c->dres + 16);
+    c->derr = (int *)(c->dres + 32);
     c->wait_limit_ns = 1000000000ULL;
     for (int b = 0; b < 2; ++b)
         for (int f = 0; f < 3; ++f) c->fld[b][f] = (char *)c->state + (size_t)(3 * b + f) * fbytes;
@@ -199,7 +199,7 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
     }
     // zero the padding once so that unused ghost edges hold finite values
     e = cudaMemsetAsync(c->state, 0, 6 * fbytes, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->dres, 0, 16 * sizeof(double) + 64, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dres, 0, 32 * sizeof(double) + 64, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
         ppf_destroy(c);

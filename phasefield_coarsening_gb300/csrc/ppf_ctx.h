@@ -25,7 +25,8 @@ struct ppf_ctx {
     double *staging;      // 3 * cells doubles, compact [z][y][x]
     double *partials;     // per-CTA partial sums
     int partials_cap;     // in doubles
-    double *dres;         // device results: [0..2] increments, [3..7] observables
+    double *dres;         // device results: [0..2] increments, [3..7] observables, [8..12] particles,
+                          // [16..19] mass-projection plan; the error word follows at dres + 32
     int *derr;            // device error word set by a kernel whose bounded wait ran out
     CUtensorMap maps[2][3];   // TMA maps of the fields of both buffers
     ppf::StepTune tune;        // launch choices of the fused step (grid, z chunk, unroll)

@@ -64,6 +64,7 @@ struct ConvArgs {
     uint16_t *zout;         // pre-activations (EPI_ACT_TRAIN), interior only
     const uint16_t *zlow;   // pre-activations of the layer below (EPI_DGRAD)
     float *partials;        // per CTA: CO bias-gradient sums, then the loss (EPI_DGRAD, EPI_LOSS)
+    double *mass_part;      // per CTA: FP64 sum of the new c (EPI_STATE)
     Geom sg;                // state geometry (EPI_STATE, EPI_LOSS)
     Fields<const float> s0; // state at the start of the call
     Fields<float> s1;       // EPI_STATE: state written; EPI_LOSS: target state (read)

@@ -14,8 +14,9 @@
 //   The A operand of tap (dz, dy, dx) is its segment started dx+1 voxels
 //   (16 bytes each) in; the B operand is that tap's CI x CO block of the
 //   weight image, loaded once per CTA.
-//   Warp roles (320 threads): warp 0 lane 0 issues the bulk copies, warp 1
-//   lane 0 issues the MMAs (and warp 1 owns the TMEM allocation), warps
+//   Warp roles (352 threads): warp 0 lane 0 issues the bulk copies, lane 0
+//   of warps 1 and 10 issue the MMAs of alternate rows (warp 1 owns the
+//   TMEM allocation), warps
 //   2-9 run the epilogue on a double-buffered TMEM accumulator (warp w
 //   reads TMEM lanes 32 (w % 4).., warps 2-5 the first half of the output
 //   channels, warps 6-9 the second), so the epilogue of one tile overlaps
@@ -62,6 +63,22 @@ __device__ __forceinline__ bool wait_or_abort(uint32_t bar, uint32_t parity, uns
     }
 }
 
+// the same with a short sleep between polls: for the many epilogue warps,
+// whose spinning would otherwise take issue slots from the MMA thread
+__device__ __forceinline__ bool wait_backoff(uint32_t bar, uint32_t parity, unsigned long long limit_ns,
+                                             volatile int *abort_flag) {
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer();
+    for (uint32_t it = 0;; ++it) {
+        __nanosleep(64);
+        if (mbar_try(bar, parity)) return true;
+        if ((it & 7u) == 7u) {
+            if (*abort_flag) return false;
+            if (globaltimer() - t0 > limit_ns) return false;
+        }
+    }
+}
+
 __device__ __forceinline__ void fail(volatile int *abort_flag, int *err, int code) {
     *abort_flag = 1;
     atomicOr(err, code);
@@ -93,11 +110,13 @@ __device__ __forceinline__ void unpack8(uint4 q, float *f) {
     }
 }
 
-// logistic function with the hardware reciprocal (rcp.approx, ~1 ulp)
+// logistic function: sigma(z) = (1 + tanh(z/2)) / 2 with the hardware
+// tanh (tanh.approx.f32, relative error about 2^-11, well below the BF16
+// rounding of every value it feeds)
 __device__ __forceinline__ float sigmoidf(float z) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + __expf(-z)));
-    return r;
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+    return fmaf(0.5f, t, 0.5f);
 }
 
 template <int NP>
@@ -121,7 +140,9 @@ __device__ __forceinline__ void store_with_images(const NNGeom &g, uint16_t *bas
     }
 }
 
-constexpr int kConvThreads = 320;   // producer warp, MMA warp, 8 epilogue warps
+constexpr int kConvThreads = 352;   // producer warp, MMA warp, 8 epilogue warps, second MMA warp
+constexpr int kMmaWarp2 = 10;
+constexpr int kEpiThreads = 256;
 
 template <int CI, int CO>
 struct ConvCfg {
@@ -134,11 +155,12 @@ struct ConvCfg {
     static constexpr int HALF = CO / 2;                  // output channels per epilogue warp
     static constexpr int OFF_W = RING * ROWB;
     static constexpr int OFF_BAR = OFF_W + WB;
-    static constexpr int NBAR = 2 * RING + 2 * ND + 2;   // full, empty, dfull, dempty, wbar, drain
+    static constexpr int NBAR = 2 * RING + 2 * ND + 3;   // full, empty, dfull, dempty, wbar, drain x2
     static constexpr int OFF_SLOT = OFF_BAR + NBAR * 8;  // TMEM base, abort flag
     static constexpr int OFF_RED = OFF_SLOT + 16;        // [8][HALF + 1] floats
     static constexpr int OFF_BIAS = OFF_RED + 8 * (HALF + 1) * 4;   // CO floats
-    static constexpr int SMEM = OFF_BIAS + CO * 4;
+    static constexpr int OFF_REDD = (OFF_BIAS + CO * 4 + 7) / 8 * 8;  // [4] doubles
+    static constexpr int SMEM = OFF_REDD + 4 * 8;
     static constexpr int TMEM_COLS = ND * NCOL <= 256 ? 256 : 512;
     static_assert(CI % 16 == 0 && CO % 16 == 0 && CO <= 32, "channel counts");
     static_assert(ND * NCOL <= 512 && NCOL <= 256, "TMEM / MMA N");
@@ -197,10 +219,11 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
         }
         for (int s = 0; s < C::ND; ++s) {
             mbar_init(dfull(s), 1);
-            mbar_init(dempty(s), kConvThreads - 64);
+            mbar_init(dempty(s), kEpiThreads);
         }
         mbar_init(wbar, 1);
         mbar_init(dbar, 1);
+        mbar_init(dbar + 8, 1);
         *abort_flag = 0;
         mbar_init_fence();
     }
@@ -253,9 +276,13 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                     atomicOr(a.err, 4);
             if (!mbar_wait(wbar, 0, a.limit_ns)) atomicOr(a.err, 4);
         }
-    } else if (warp == 1) {
-        // ---------------- MMA issuer: one D tile per input row ----------------
+    } else if (warp == 1 || warp == kMmaWarp2) {
+        // ---------------- MMA issuers: one D tile per input row; warp 1
+        // takes the even rows, warp 10 the odd ones, so that one thread's
+        // waits and bookkeeping overlap the other's MMAs ----------------
         if (lane == 0) {
+            const uint32_t mine = warp == 1 ? 0u : 1u;
+            const uint32_t mydbar = warp == 1 ? dbar : dbar + 8;
             const uint32_t idesc = idesc_bf16(128, C::NCOL, false, false);
             // descriptors of slot 0 and of the weight image; every operand
             // below is one of these plus a byte offset / 16 (no carry: all
@@ -269,6 +296,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
             for (int it = blockIdx.x; ok && it < a.items; it += gridDim.x) {
                 const Item w = item_of(g, a.yc, it);
                 for (int r = w.y0 - 1; r <= w.y1; ++r, ++q) {
+                    if ((q & 1u) != mine) continue;
                     const uint32_t s = q % C::RING, ds = q % C::ND;
                     if (!wait_or_abort(full(s), (q / C::RING) & 1, a.limit_ns, abort_flag) ||
                         (q >= (uint32_t)C::ND &&
@@ -295,11 +323,11 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                 }
             }
             // drain: all issued MMAs complete before TMEM is released
-            mma_commit(dbar);
-            if (!mbar_wait(dbar, 0, a.limit_ns)) atomicOr(a.err, 4);
+            mma_commit(mydbar);
+            if (!mbar_wait(mydbar, 0, a.limit_ns)) atomicOr(a.err, 4);
         }
     } else {
-        // ---------------- epilogue: 8 warps; TMEM lane quarter = warp % 4,
+        // ---------------- epilogue: warps 2-9; TMEM lane quarter = warp % 4,
         // output channels [c0, c0 + HALF) by warp group ----------------
         const int ew = warp - 2;
         const int quarter = warp & 3;
@@ -311,6 +339,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
         float sums[HALF + 1];
 #pragma unroll
         for (int c = 0; c <= HALF; ++c) sums[c] = 0.f;
+        double mass = 0.0;
         uint32_t q = 0;
         bool ok = true;
         for (int it = blockIdx.x; ok && it < a.items; it += gridDim.x) {
@@ -343,9 +372,9 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                         s1v[2] = a.s1.c[sa];
                     }
                 }
-                if (!wait_or_abort(dfull((qy - 1) % C::ND), ((qy - 1) / C::ND) & 1, a.limit_ns, abort_flag) ||
-                    !wait_or_abort(dfull(qy % C::ND), (qy / C::ND) & 1, a.limit_ns, abort_flag) ||
-                    !wait_or_abort(dfull((qy + 1) % C::ND), ((qy + 1) / C::ND) & 1, a.limit_ns, abort_flag)) {
+                if (!wait_backoff(dfull((qy - 1) % C::ND), ((qy - 1) / C::ND) & 1, a.limit_ns, abort_flag) ||
+                    !wait_backoff(dfull(qy % C::ND), (qy / C::ND) & 1, a.limit_ns, abort_flag) ||
+                    !wait_backoff(dfull((qy + 1) % C::ND), ((qy + 1) / C::ND) & 1, a.limit_ns, abort_flag)) {
                     fail(abort_flag, a.err, 1);
                     ok = false;
                     break;
@@ -431,6 +460,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                         a.s1.eS[sa] = nv[0];
                         a.s1.eL[sa] = nv[1];
                         a.s1.c[sa] = nv[2];
+                        mass += (double)nv[2];
                         if (ax != kNone) {
                             const int64_t b = sg.at(ax, y, z);
                             a.s1.eS[b] = nv[0]; a.s1.eL[b] = nv[1]; a.s1.c[b] = nv[2];
@@ -461,6 +491,16 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                 }
             }
         }
+        if (EPI == EPI_STATE) {
+            // deterministic per-CTA FP64 sum of the new c (warps 2-5 hold it)
+            double* redd = reinterpret_cast<double *>(smem + C::OFF_REDD);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mass += __shfl_xor_sync(0xffffffffu, mass, o);
+            if (lane == 0 && ew < 4) redd[ew] = mass;
+            asm volatile("bar.sync 1, %0;" ::"r"(kEpiThreads) : "memory");
+            if (ew == 0 && lane == 0 && a.mass_part)
+                a.mass_part[blockIdx.x] = ((redd[0] + redd[1]) + redd[2]) + redd[3];
+        }
         if (EPI == EPI_DGRAD || EPI == EPI_LOSS) {
             // deterministic per-CTA sums: warp shuffle, then the four warps
             // of each column group in a fixed order
@@ -471,7 +511,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                 for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
                 if (lane == 0) red[ew * (HALF + 1) + c] = sv;
             }
-            asm volatile("bar.sync 1, %0;" ::"r"(kConvThreads - 64) : "memory");
+            asm volatile("bar.sync 1, %0;" ::"r"(kEpiThreads) : "memory");
             if (ew == 0) {
                 float *dst = a.partials + (int64_t)blockIdx.x * (CO + 1);
                 for (int c = lane; c < CO; c += 32) {

@@ -72,39 +72,14 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
     return *reinterpret_cast<const uint32_t *>(&h);
 }
 
-// state (FP32, stencil layout) -> 16-channel BF16 features with halo images
-__global__ void __launch_bounds__(kNT) features_kernel(Geom sg, Fields<const float> s, NNGeom g, uint16_t *act,
-                                                       float cS, float cL, float kc) {
-    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
-    for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kNT) {
-        const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((int64_t)g.nx * g.ny));
-        const int64_t a = sg.at(x, y, z);
-        const float eS = s.eS[a], eL = s.eL[a], c = s.c[a];
-        const float s2 = eS * eS, l2 = eL * eL;
-        const float h = s2 / fmaxf(s2 + l2, 1e-30f);
-        const float f2 = (c - (cL + (cS - cL) * h)) * kc;
-        const uint4 v[2] = {make_uint4(pack2(eS, eL), pack2(f2, 0.f), 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
-        int ox[3], oy[3], oz[3];
-        const int kx = face_images(x, g.nx, g.bc, ox), ky = face_images(y, g.ny, g.bc, oy),
-                  kz = face_images(z, g.nz, g.bc, oz);
-        for (int cz = 0; cz < kz; ++cz)
-            for (int cy = 0; cy < ky; ++cy)
-                for (int cx = 0; cx < kx; ++cx) {
-                    const int64_t p = g.p(ox[cx], oy[cy], oz[cz]);
-                    for (int j = 0; j < 2; ++j)
-                        *reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(act) + ((int64_t)j * g.Pst + p) * 16) = v[j];
-                }
-    }
+// the halo image of interior coordinate x, or kNone (periodic: x=0 -> n,
+// x=n-1 -> -1; no-flux: x=0 -> -1, x=n-1 -> n)
+constexpr int kNone = -0x40000000;
+__device__ __forceinline__ int image_of(int x, int n, int bc) {
+    return x == 0 ? (bc == 0 ? n : -1) : x == n - 1 ? (bc == 0 ? -1 : n) : kNone;
 }
 
-// FP64 per-CTA sums of c over the interior
-__global__ void __launch_bounds__(kNT) csum_kernel(Geom sg, const float *c, double *partials) {
-    const int64_t n = (int64_t)sg.nx * sg.ny * sg.nz;
-    double s = 0;
-    for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kNT) {
-        const int x = (int)(i % sg.nx), y = (int)((i / sg.nx) % sg.ny), z = (int)(i / ((int64_t)sg.nx * sg.ny));
-        s += (double)c[sg.at(x, y, z)];
-    }
+__device__ __forceinline__ void block_sum_to(double s, double *out) {
     __shared__ double red[kNT / 32];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
@@ -112,30 +87,102 @@ __global__ void __launch_bounds__(kNT) csum_kernel(Geom sg, const float *c, doub
     if (threadIdx.x == 0) {
         double t = 0;
         for (int w = 0; w < kNT / 32; ++w) t += red[w];
-        partials[blockIdx.x] = t;
+        *out = t;
     }
 }
 
-// c += q_i 2^-24 with q_i = floor((i+1) r) - floor(i r), r = (target - sum) / (n 2^-24):
-// the q_i add up to floor(n r) exactly, spread evenly over the cells
-__global__ void __launch_bounds__(kNT) distribute_kernel(Geom sg, float *c, const double *target, const double *sum) {
-    const int64_t n = (int64_t)sg.nx * sg.ny * sg.nz;
-    const double u = 5.9604644775390625e-08;   // 2^-24
-    const double r = (*target - *sum) / ((double)n * u);
-    if (!(fabs(r) < 1e12)) return;             // nothing sensible to spread (non-finite sums)
-    for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kNT) {
-        const double q = floor((double)(i + 1) * r) - floor((double)i * r);
-        if (q == 0.0) continue;
-        const int x = (int)(i % sg.nx), y = (int)((i / sg.nx) % sg.ny), z = (int)(i / ((int64_t)sg.nx * sg.ny));
-        const int64_t a = sg.at(x, y, z);
-        const float v = (float)((double)c[a] + q * u);
-        c[a] = v;
-        int ox[3], oy[3], oz[3];
-        const int kx = face_images(x, sg.nx, sg.bc, ox), ky = face_images(y, sg.ny, sg.bc, oy),
-                  kz = face_images(z, sg.nz, sg.bc, oz);
-        for (int k = 1; k < kx; ++k) c[sg.at(ox[k], y, z)] = v;
-        for (int k = 1; k < ky; ++k) c[sg.at(x, oy[k], z)] = v;
-        for (int k = 1; k < kz; ++k) c[sg.at(x, y, oz[k])] = v;
+// state (FP32, stencil layout) -> first channel plane of the 16-channel
+// BF16 features (etaS, etaL, composition feature; channels 8..15 live in
+// the second plane, zero from allocation and never written), with every
+// halo image; also the per-CTA FP64 sum of c (the mass before the call).
+// One block per x row (grid-stride over rows).
+__global__ void __launch_bounds__(kNT) features_kernel(Geom sg, Fields<const float> s, NNGeom g, uint16_t *act,
+                                                       float cS, float cL, float kc, double *mass_part) {
+    double m = 0;
+    const int nrows = g.ny * g.nz;
+    for (int rr = blockIdx.x; rr < nrows; rr += gridDim.x) {
+        const int y = rr % g.ny, z = rr / g.ny;
+        const int ay = image_of(y, g.ny, g.bc), az = image_of(z, g.nz, g.bc);
+        const int64_t a0 = sg.at(0, y, z);
+        for (int x = threadIdx.x; x < g.nx; x += kNT) {
+            const float eS = s.eS[a0 + x], eL = s.eL[a0 + x], c = s.c[a0 + x];
+            m += (double)c;
+            const float s2 = eS * eS, l2 = eL * eL;
+            const float h = s2 / fmaxf(s2 + l2, 1e-30f);
+            const float f2 = (c - (cL + (cS - cL) * h)) * kc;
+            const uint4 v = make_uint4(pack2(eS, eL), pack2(f2, 0.f), 0u, 0u);
+            const int ax = image_of(x, g.nx, g.bc);
+            for (int k = 0; k < 8; ++k) {
+                const int xx = (k & 1) ? ax : x, yy = (k & 2) ? ay : y, zz = (k & 4) ? az : z;
+                if (xx == kNone || yy == kNone || zz == kNone) continue;
+                *reinterpret_cast<uint4 *>(reinterpret_cast<unsigned char *>(act) + g.p(xx, yy, zz) * 16) = v;
+            }
+        }
+    }
+    block_sum_to(m, mass_part + blockIdx.x);
+}
+
+// FP64 per-CTA sums of c over the interior, one block per x row
+__global__ void __launch_bounds__(kNT) csum_kernel(Geom sg, const float *c, double *partials) {
+    double m = 0;
+    const int nrows = sg.ny * sg.nz;
+    for (int rr = blockIdx.x; rr < nrows; rr += gridDim.x) {
+        const float *row = c + sg.at(0, rr % sg.ny, rr / sg.ny);
+        for (int x = threadIdx.x; x < sg.nx; x += kNT) m += (double)row[x];
+    }
+    block_sum_to(m, partials + blockIdx.x);
+}
+
+// The projection moves sum(c) by R = round((target - sum) / 2^-24) units of
+// 2^-24: every cell by `base` units and `rem` cells by one more, where
+// base = floor(R / n), rem = R - base n in [0, n); the cells taking the
+// extra unit are i_k = ceil((k+1) n / rem) - 1, k < rem (evenly spread: the
+// cells where floor((i+1) rem / n) steps up).
+struct MassPlan {
+    double target, sum;
+    long long base, rem;
+};
+
+__global__ void plan_kernel(MassPlan *mp, long long n) {
+    const double d = (mp->target - mp->sum) * 16777216.0;   // in units of 2^-24
+    long long R = 0;
+    if (fabs(d) < 4.0e18) R = llrint(d);                     // non-finite or absurd: leave c alone
+    long long base = R / n, rem = R % n;
+    if (rem < 0) {
+        rem += n;
+        base -= 1;
+    }
+    mp->base = base;
+    mp->rem = rem;
+}
+
+__device__ __forceinline__ void put_c(const Geom &sg, float *c, int x, int y, int z, double add) {
+    const int64_t a = sg.at(x, y, z);
+    const float v = (float)((double)c[a] + add);
+    c[a] = v;
+    const int ax = image_of(x, sg.nx, sg.bc), ay = image_of(y, sg.ny, sg.bc), az = image_of(z, sg.nz, sg.bc);
+    if (ax != kNone) c[sg.at(ax, y, z)] = v;
+    if (ay != kNone) c[sg.at(x, ay, z)] = v;
+    if (az != kNone) c[sg.at(x, y, az)] = v;
+}
+
+__global__ void __launch_bounds__(kNT) dense_kernel(Geom sg, float *c, const MassPlan *mp) {
+    const long long base = mp->base;
+    if (base == 0) return;
+    const double add = (double)base * 5.9604644775390625e-08;
+    const int nrows = sg.ny * sg.nz;
+    for (int rr = blockIdx.x; rr < nrows; rr += gridDim.x) {
+        const int y = rr % sg.ny, z = rr / sg.ny;
+        for (int x = threadIdx.x; x < sg.nx; x += kNT) put_c(sg, c, x, y, z, add);
+    }
+}
+
+__global__ void __launch_bounds__(kNT) sparse_kernel(Geom sg, float *c, const MassPlan *mp, long long n) {
+    const long long rem = mp->rem;
+    for (long long k = blockIdx.x * (long long)kNT + threadIdx.x; k < rem; k += (long long)gridDim.x * kNT) {
+        const long long i = ((k + 1) * n + rem - 1) / rem - 1;
+        const int x = (int)(i % sg.nx), y = (int)((i / sg.nx) % sg.ny), z = (int)(i / ((long long)sg.nx * sg.ny));
+        put_c(sg, c, x, y, z, 5.9604644775390625e-08);
     }
 }
 
@@ -201,7 +248,8 @@ struct ppf_surrogate {
     NNGeom g{};
     uint16_t *feat = nullptr, *act[5] = {}, *zp[5] = {}, *g16 = nullptr, *gw[2] = {};
     float *wpart = nullptr, *bpart = nullptr;
-    double *dscal = nullptr;     // [0] loss, [1] mass target, [2] mass sum
+    double *mpart = nullptr;     // per-CTA sums of c after a call (output layer)
+    double *dscal = nullptr;     // [0] loss
     double *dpart = nullptr;
     int dpart_cap = 0;
     float *scratch = nullptr;    // predictions: zero state + output state
@@ -306,12 +354,19 @@ int run_conv(ppf_surrogate *s, ppf_ctx *c, int ci, int co, int epi, const ConvAr
     return PPF_OK;
 }
 
+MassPlan *plan_of(ppf_ctx *c) { return reinterpret_cast<MassPlan *>(c->dres + 16); }
+
+int row_blocks(const ppf_ctx *c) { return (int)std::min<int64_t>((int64_t)c->ny * c->nz, 8LL * c->num_sms); }
+
+// features of the current state; the mass before the call goes to the plan's target
 int features(ppf_surrogate *s, ppf_ctx *c) {
-    const int64_t n = (int64_t)c->nz * c->ny * c->nx;
-    const int nb = (int)std::min<int64_t>((n + kNT - 1) / kNT, 8LL * s->num_sms);
+    const int nb = row_blocks(c);
+    int rc = ensure_partials(c, nb);
+    if (rc) return rc;
     features_kernel<<<nb, kNT, 0, c->stream>>>(c->g, cur_fields(c), s->g, s->feat, (float)s->cfg.c_solid,
-                                               (float)s->cfg.c_liquid, (float)s->cfg.in_scale_c);
+                                               (float)s->cfg.c_liquid, (float)s->cfg.in_scale_c, c->partials);
     SCU(cudaGetLastError());
+    SCU(launch_final_sum(c->partials, nb, 1, 1, &plan_of(c)->target, c->stream));
     return PPF_OK;
 }
 
@@ -404,8 +459,7 @@ int pack_all(ppf_surrogate *s, cudaStream_t st) {
 }
 
 int mass_sum(ppf_ctx *c, double *out) {
-    const int64_t n = (int64_t)c->nz * c->ny * c->nx;
-    const int nb = (int)std::min<int64_t>((n + kNT - 1) / kNT, 4LL * c->num_sms);
+    const int nb = row_blocks(c);
     int rc = ensure_partials(c, nb);
     if (rc) return rc;
     csum_kernel<<<nb, kNT, 0, c->stream>>>(c->g, (const float *)c->fld[c->cur_c][2], c->partials);
@@ -414,14 +468,20 @@ int mass_sum(ppf_ctx *c, double *out) {
     return PPF_OK;
 }
 
-// project sum(c) onto *target (device double), two passes
-int project(ppf_ctx *c, const double *target, double *sum) {
-    const int64_t n = (int64_t)c->nz * c->ny * c->nx;
-    const int nb = (int)std::min<int64_t>((n + kNT - 1) / kNT, 8LL * c->num_sms);
+// move sum(c) onto the plan's target; `have_sum`: the plan's sum is already
+// that of the current state
+int project(ppf_ctx *c, bool have_sum) {
+    MassPlan *mp = plan_of(c);
+    const long long n = (long long)c->nz * c->ny * c->nx;
+    float *cc = (float *)c->fld[c->cur_c][2];
     for (int pass = 0; pass < 2; ++pass) {
-        int rc = mass_sum(c, sum);
-        if (rc) return rc;
-        distribute_kernel<<<nb, kNT, 0, c->stream>>>(c->g, (float *)c->fld[c->cur_c][2], target, sum);
+        if (pass > 0 || !have_sum) {
+            int rc = mass_sum(c, &mp->sum);
+            if (rc) return rc;
+        }
+        plan_kernel<<<1, 1, 0, c->stream>>>(mp, n);
+        dense_kernel<<<row_blocks(c), kNT, 0, c->stream>>>(c->g, cc, mp);
+        sparse_kernel<<<4 * c->num_sms, kNT, 0, c->stream>>>(c->g, cc, mp, n);
         SCU(cudaGetLastError());
     }
     return PPF_OK;
@@ -490,6 +550,7 @@ extern "C" int ppf_surrogate_create(const ppf_surrogate_config *cfg, ppf_surroga
               cudaMalloc(&s->mom1, pb) == cudaSuccess && cudaMalloc(&s->mom2, pb) == cudaSuccess &&
               cudaMalloc(&s->wpart, (size_t)s->wgrad_grid * 27 * 32 * 32 * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&s->bpart, (size_t)2 * s->num_sms * 33 * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&s->mpart, (size_t)2 * s->num_sms * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&s->dscal, 8 * sizeof(double)) == cudaSuccess;
     for (int l = 0; ok && l < kLayers; ++l)
         ok = cudaMalloc(&s->wf[l], 27 * s->ci[l] * s->co[l] * 2) == cudaSuccess &&
@@ -521,6 +582,7 @@ extern "C" int ppf_surrogate_destroy(ppf_surrogate *s) {
     cudaFree(s->mom2);
     cudaFree(s->wpart);
     cudaFree(s->bpart);
+    cudaFree(s->mpart);
     cudaFree(s->dscal);
     delete s;
     return PPF_OK;
@@ -614,6 +676,7 @@ extern "C" int ppf_surrogate_predict(ppf_surrogate *s, ppf_ctx *c, double *out3)
     ConvArgs a = conv_args(s, c, 5, s->act[4], s->wf[5]);
     a.s0 = {z0, z0 + T, z0 + 2 * T};
     a.s1 = {o, o + T, o + 2 * T};
+    a.mass_part = s->mpart;
     if ((rc = run_conv(s, c, s->ci[5], 16, EPI_STATE, a))) return rc;
     SCU(launch_unpack<float>(c->g, Fields<const float>{o, o + T, o + 2 * T}, s->stage, c->stream));
     SCU(cudaMemcpyAsync(out3, s->stage, (size_t)3 * c->nz * c->ny * c->nx * sizeof(double), cudaMemcpyDeviceToHost,
@@ -627,19 +690,19 @@ extern "C" int ppf_surrogate_advance(ppf_surrogate *s, ppf_ctx *c, int ncalls) {
     if (ncalls < 0) return serr(PPF_EINVAL, "negative call count");
     int rc = ensure_ws(s, c, false);
     if (rc) return rc;
-    double *target = c->dres + 13, *sum = c->dres + 14;
     for (int k = 0; k < ncalls; ++k) {
-        if ((rc = mass_sum(c, target))) return rc;
-        if ((rc = forward_hidden(s, c, false))) return rc;
+        if ((rc = forward_hidden(s, c, false))) return rc;     // features: mass before the call
         const int ie = c->cur_eta, ic = c->cur_c;
         ConvArgs a = conv_args(s, c, 5, s->act[4], s->wf[5]);
         a.s0 = cur_fields(c);
         a.s1 = {(float *)c->fld[1 - ie][0], (float *)c->fld[1 - ie][1], (float *)c->fld[1 - ic][2]};
+        a.mass_part = s->mpart;
         if ((rc = run_conv(s, c, s->ci[5], 16, EPI_STATE, a))) return rc;
+        SCU(launch_final_sum(s->mpart, s->conv_grid[s->ci[5] == 32][0], 1, 1, &plan_of(c)->sum, c->stream));
         c->cur_eta = 1 - ie;
         c->cur_c = 1 - ic;
         c->steps += s->cfg.k_steps;
-        if ((rc = project(c, target, sum))) return rc;
+        if ((rc = project(c, true))) return rc;
     }
     return PPF_OK;
 }
@@ -649,9 +712,8 @@ extern "C" int ppf_mass_project(ppf_ctx *c, double target_mass) {
     if (c->prec != PPF_F32) return serr(PPF_EINVAL, "mass projection applies to FP32 contexts");
     if (!c->uploaded) return serr(PPF_ESTATE, "no state uploaded");
     if (!std::isfinite(target_mass)) return serr(PPF_EINVAL, "target mass must be finite");
-    double *target = c->dres + 13, *sum = c->dres + 14;
-    SCU(cudaMemcpyAsync(target, &target_mass, sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    int rc = project(c, target, sum);
+    SCU(cudaMemcpyAsync(&plan_of(c)->target, &target_mass, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int rc = project(c, false);
     if (rc) return rc;
     SCU(cudaStreamSynchronize(c->stream));
     return check_device_error(c);

@@ -153,6 +153,62 @@ def cpu_baseline_sample(state, cells):
             "sample": f"{steps} time steps of the 256^3 workload, oracle restatement (C, OpenMP), {ncores} threads"}
 
 
+SURROGATE_WEIGHTS = ("surrogate_w16_k50.npz", "surrogate_w16_k200.npz")
+
+
+def surrogate_section(state, shape):
+    """The learned surrogate + stencil corrector against the plain FP32
+    stencil on the same 256^3 state: simulated time per wall second of both
+    arms (device-synchronised host clock around each cycle), the largest
+    relative errors of mean particle radius, solid fraction and free energy
+    over the run, the solute-mass drift, and the tensor throughput of one
+    surrogate call.  One entry per committed trained network."""
+    import numpy as np
+
+    import phasefield_coarsening_gb300 as ppf
+    from phasefield_coarsening_gb300 import surrogate as S
+
+    cells = int(np.prod(shape))
+    peak = None
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        peak = float(json.load(open(p)).get("bf16_tflops_sustained", 0)) or None
+    out = []
+    for name in SURROGATE_WEIGHTS:
+        path = os.path.join(REPO, "phasefield_coarsening_gb300", "weights", name)
+        if not os.path.exists(path):
+            continue
+        net = S.load(path)
+        cfg = net.config
+        res = S.judge(net, state, cycles=12, calls=10, corrector_steps=50, warmup=500)
+        res.pop("trajectory")
+        sim = ppf.Simulation(shape, ppf.params_default(dt=DT), "periodic", "f32")
+        sim.upload(*state)
+        net.advance(sim, 2)
+        sim.sync()
+        w0 = time.perf_counter()
+        net.advance(sim, 10)
+        sim.sync()
+        call_s = (time.perf_counter() - w0) / 10
+        sim.close()
+        w = cfg["width"]
+        chans = [16, w, w, w, w, w, 16]
+        flop = 2 * 27 * sum(chans[i] * chans[i + 1] for i in range(6)) * cells
+        tf = flop / call_s / 1e12
+        out.append({
+            "weights": name, "width": w, "k_steps": cfg["k_steps"], "calls_per_cycle": 10, "corrector_steps": 50,
+            "sim_time_per_wall_s": res["sim_time_per_wall_s"], "speedup_vs_stencil": round(res["speedup"], 3),
+            "max_rel_err": res["max_rel_err"], "mass_drift": res["mass_drift"], "steps": res["steps"],
+            "fallbacks": res["fallbacks"], "ms_per_call": round(call_s * 1e3, 3),
+            "roofline": {"bound": "tensor", "achieved": round(tf, 1), "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(tf / peak, 4) if peak else None,
+                         "flop_per_call": flop, "what": "executed BF16 MMA FLOPs of one call over its whole "
+                                                       "duration (features, 6 convolutions, mass projection)"},
+        })
+        net.close()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -263,6 +319,8 @@ def run_ours(args):
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample((eS, eL, c), cells)
+        if not args.no_surrogate:
+            line["surrogate"] = surrogate_section((eS, eL, c), shape)
         print(json.dumps(line), flush=True)
     sim.close()
     if world > 1:
@@ -417,6 +475,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--workload", choices=[WORKLOAD, "ensemble64"], default=WORKLOAD)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

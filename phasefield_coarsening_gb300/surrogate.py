@@ -1,0 +1,254 @@
+"""Learned time stepping on top of the explicit step.
+
+The surrogate (include/ppf.h, ppf_surrogate_*) advances an FP32 state by
+k explicit steps of the reference's sweep_fields (phasefield.c:301-403)
+in one call.  This module holds what surrounds it:
+
+* PairStream -- training pairs (state, state after k stencil steps) along
+  stencil trajectories of seeded sphere microstructures (periodic FP32
+  domains whose x edge is a multiple of 128);
+* calibrate / train -- output scales from the data, and on-device training
+  with Adam through the project's own forward and backward kernels;
+* Stepper -- the production form: cycles of `calls` surrogate calls
+  followed by `corrector_steps` stencil steps (the corrector), with the
+  solute mass projected in FP64 after every call; a cycle whose result
+  fails the checks (non-finite cells, free energy rising, solid fraction
+  drifting) is redone with the stencil alone (the fallback);
+* judge -- the surrogate arm against the plain stencil from the same
+  state: mean particle radius, solid fraction, free energy, solute mass.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from . import Simulation, Surrogate, ic, params_default
+
+DT = 0.8 / (6.0 * 1e-14)       # 0.8 of the explicit limit dx^2 / (6 DL)
+
+
+def microstructure(shape, seed, vf=0.3, radius=("lognormal", 5.0, 0.3)):
+    """Seeded non-overlapping spheres at solid fraction `vf` (etaS, etaL, c)."""
+    eS, eL, c, _ = ic.generate(shape, radius=radius, vf=min(vf, 0.34), seed=seed)
+    return eS, eL, c
+
+
+class PairStream:
+    """Consecutive (state, state after k steps) pairs along stencil
+    trajectories; a new microstructure every `segment` pairs, first relaxed
+    by `warmup` stencil steps."""
+
+    def __init__(self, shape=(64, 128, 128), k=50, seed=0, warmup=200, segment=25, vf=(0.15, 0.34),
+                 params=None):
+        self.shape, self.k, self.seed, self.warmup, self.segment, self.vf = tuple(shape), k, seed, warmup, segment, vf
+        self.params = params if params is not None else params_default(dt=DT)
+        self.a = Simulation(self.shape, self.params, "periodic", "f32")
+        self.b = Simulation(self.shape, self.params, "periodic", "f32")
+        self.count = 0
+        self.domains = 0
+
+    def close(self):
+        self.a.close()
+        self.b.close()
+
+    def next(self):
+        if self.count % self.segment == 0:
+            rng = np.random.default_rng([self.seed, self.domains])
+            self.a.upload(*microstructure(self.shape, seed=int(rng.integers(1 << 30)), vf=float(rng.uniform(*self.vf))))
+            self.a.step(self.warmup)
+            self.domains += 1
+        else:
+            self.a.copy_from(self.b)
+        self.b.copy_from(self.a)
+        self.b.step(self.k)
+        self.count += 1
+        return self.a, self.b
+
+
+def calibrate(stream: PairStream, n=3):
+    """Root-mean-square change of etaS, etaL, c over k steps (the output scales)."""
+    acc = np.zeros(3)
+    for _ in range(n):
+        a, b = stream.next()
+        x, y = a.download(), b.download()
+        acc += [float(np.mean((q - p) ** 2)) for p, q in zip(x, y)]
+    return [float(math.sqrt(v / n)) for v in acc]
+
+
+def train(net: Surrogate, stream: PairStream, iters: int, lr=1e-3, lr_final=1e-4, log_every=100):
+    """Adam over `iters` stream pairs, learning rate decaying geometrically
+    from lr to lr_final; returns [(iteration, loss)]."""
+    log = []
+    for i in range(iters):
+        a, b = stream.next()
+        f = i / max(1, iters - 1)
+        lr_i = lr * (lr_final / lr) ** f
+        want = (i % log_every == 0) or i == iters - 1
+        loss = net.train_step(a, b, lr=lr_i, want_loss=want)
+        if want:
+            log.append((i, loss))
+    return log
+
+
+class Stepper:
+    """Surrogate + corrector time stepping of one FP32 state."""
+
+    def __init__(self, net: Surrogate, sim: Simulation, calls=10, corrector_steps=50, vf_tol=0.005,
+                 f_tol=1e-7, check=True):
+        self.net, self.sim = net, sim
+        self.k = int(net.config["k_steps"])
+        self.calls, self.corrector_steps, self.vf_tol, self.f_tol, self.check = \
+            calls, corrector_steps, vf_tol, f_tol, check
+        self.snap = Simulation(sim.shape, sim.params, "periodic" if sim.bc == 0 else "noflux", "f32") if check else None
+        self.mass = sim.reduce()["mass"]       # conserved by the model: every cycle ends on it
+        self.cycles = 0
+        self.fallbacks = 0
+
+    @property
+    def steps_per_cycle(self):
+        return self.calls * self.k + self.corrector_steps
+
+    def close(self):
+        if self.snap is not None:
+            self.snap.close()
+
+    def cycle(self):
+        s = self.sim
+        if self.check:
+            self.snap.copy_from(s)
+            st0 = s.reduce()
+        self.net.advance(s, self.calls)
+        s.step(self.corrector_steps)
+        self.cycles += 1
+        if self.check:
+            st1 = s.reduce()
+            f0, f1 = st0["free_energy"], st1["free_energy"]
+            bad = (st1["nonfinite"] != 0 or not math.isfinite(f1) or f1 > f0 + self.f_tol * abs(f0) or
+                   abs(st1["solid"] - st0["solid"]) > self.vf_tol * max(st0["solid"], 1.0))
+            if bad:
+                s.copy_from(self.snap)
+                s.step(self.steps_per_cycle)
+                self.fallbacks += 1
+        s.mass_project(self.mass)
+        return self.steps_per_cycle
+
+
+def judge(net: Surrogate, state, cycles=10, calls=10, corrector_steps=50, warmup=0, threshold=0.5,
+          params=None, check=True):
+    """Advance `state` with the surrogate + corrector and with the plain FP32
+    stencil for the same simulated time; after every cycle compare mean
+    particle radius, solid fraction and free energy.  Returns a dict of the
+    largest relative errors, the surrogate arm's solute-mass drift and both
+    arms' simulated time per wall second (device-synchronised timing)."""
+    shape = state[0].shape
+    prm = params if params is not None else params_default(dt=DT)
+    ref = Simulation(shape, prm, "periodic", "f32")
+    sur = Simulation(shape, prm, "periodic", "f32")
+    ref.upload(*state)
+    if warmup:
+        ref.step(warmup)
+    sur.copy_from(ref)
+    m0 = sur.reduce()["mass"]
+    stepper = Stepper(net, sur, calls=calls, corrector_steps=corrector_steps, check=check)
+    err = {"rbar": 0.0, "solid": 0.0, "free_energy": 0.0}
+    t_sur = t_ref = 0.0
+    steps = 0
+    rows = []
+    for _ in range(cycles):
+        sur.sync()
+        w0 = time.perf_counter()
+        n = stepper.cycle()
+        sur.sync()
+        t_sur += time.perf_counter() - w0
+        w0 = time.perf_counter()
+        ref.step(n)
+        ref.sync()
+        t_ref += time.perf_counter() - w0
+        steps += n
+        ps, pr = sur.particles(threshold), ref.particles(threshold)
+        ss, sr_ = sur.reduce(), ref.reduce()
+        e = {"rbar": abs(ps["mean_radius"] / pr["mean_radius"] - 1.0) if pr["mean_radius"] else 0.0,
+             "solid": abs(ss["solid"] / sr_["solid"] - 1.0),
+             "free_energy": abs(ss["free_energy"] / sr_["free_energy"] - 1.0)}
+        for kk in err:
+            err[kk] = max(err[kk], e[kk])
+        rows.append({"steps": steps, "rbar_sur": ps["mean_radius"], "rbar_ref": pr["mean_radius"],
+                     "count_sur": ps["count"], "count_ref": pr["count"], **{"err_" + kk: v for kk, v in e.items()}})
+    m1 = sur.reduce()["mass"]
+    dt = prm.dt
+    out = {"max_rel_err": err, "mass_drift": abs(m1 / m0 - 1.0), "steps": steps, "cycles": cycles,
+           "fallbacks": stepper.fallbacks, "sim_time_per_wall_s": {"surrogate": steps * dt / t_sur,
+                                                                    "stencil": steps * dt / t_ref},
+           "speedup": t_ref / t_sur, "trajectory": rows}
+    stepper.close()
+    ref.close()
+    sur.close()
+    return out
+
+
+def save(net: Surrogate, path: str, **meta):
+    """Parameters and configuration of a trained surrogate (.npz)."""
+    cfg = net.config
+    np.savez(path, params=net.get_params(), width=cfg["width"], k_steps=cfg["k_steps"],
+             out_scale=np.asarray(cfg["out_scale"]), in_scale_c=cfg["in_scale_c"], c_solid=cfg["c_solid"],
+             c_liquid=cfg["c_liquid"], loss_weight=np.asarray(cfg["loss_weight"]),
+             meta=np.asarray(repr(meta)))
+
+
+def load(path: str) -> Surrogate:
+    z = np.load(path, allow_pickle=False)
+    net = Surrogate(width=int(z["width"]), k_steps=int(z["k_steps"]), out_scale=[float(v) for v in z["out_scale"]],
+                    in_scale_c=float(z["in_scale_c"]), c_solid=float(z["c_solid"]), c_liquid=float(z["c_liquid"]),
+                    loss_weight=[float(v) for v in z["loss_weight"]])
+    net.set_params(z["params"])
+    return net
+
+
+def fit(width=16, k=50, iters=2000, shape=(64, 128, 128), seed=1, lr=1e-3, lr_final=1e-4, log_every=250):
+    """Train a fresh network on stencil trajectories (output scales from
+    the data, zero-initialised output layer); returns (net, log)."""
+    stream = PairStream(shape=shape, k=k, seed=seed)
+    try:
+        scales = calibrate(stream, n=3)
+        net = Surrogate(width=width, k_steps=k, out_scale=scales)
+        net.set_params(init_params(width, seed=seed))
+        log = train(net, stream, iters, lr=lr, lr_final=lr_final, log_every=log_every)
+    finally:
+        stream.close()
+    return net, log
+
+
+def init_params(width, seed=0):
+    """Seeded initial parameters: uniform weights of variance 1/fan-in over
+    the used input channels, zero output layer (the network starts as the
+    identity map), zero biases."""
+    rng = np.random.default_rng(seed)
+    chans = [16, width, width, width, width, width, 16]
+    parts = []
+    for li in range(6):
+        ci, co = chans[li], chans[li + 1]
+        ci_used = 3 if li == 0 else ci
+        W = np.zeros((27, co, ci))
+        if li < 5:
+            a = math.sqrt(3.0 / (27 * ci_used))
+            W[:, :, :ci_used] = rng.uniform(-a, a, size=(27, co, ci_used))
+        parts += [W.ravel(), np.zeros(co)]
+    return np.concatenate(parts).astype(np.float32)
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="train a surrogate on stencil trajectories and save it")
+    ap.add_argument("--width", type=int, default=16)
+    ap.add_argument("--k", type=int, default=50)
+    ap.add_argument("--iters", type=int, default=2000)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--out", required=True)
+    a = ap.parse_args()
+    t0 = time.time()
+    net, log = fit(width=a.width, k=a.k, iters=a.iters, seed=a.seed)
+    save(net, a.out, iters=a.iters, seed=a.seed, train_s=round(time.time() - t0, 1), log=log)
+    print(json.dumps({"out": a.out, "train_s": round(time.time() - t0, 1), "log": log}))

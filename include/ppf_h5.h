@@ -63,6 +63,13 @@ int ppf_h5_write3d(const char *path, int n, const char *const *names,
                    const double *const *data, const int64_t dims[3],
                    int dtype, const int64_t *chunk);
 
+/* Same, plus one float64 dataset `meta_name` of shape (1, 1, nmeta) holding
+ * `meta` (contiguous, little-endian host doubles); used for the program's
+ * restart record.  Readers that look datasets up by name are unaffected. */
+int ppf_h5_write3d_meta(const char *path, int n, const char *const *names, const double *const *data,
+                        const int64_t dims[3], int dtype, const int64_t *chunk, const char *meta_name,
+                        const double *meta, int nmeta);
+
 const char *ppf_h5_last_error(void);
 
 #ifdef __cplusplus

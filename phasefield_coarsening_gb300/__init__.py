@@ -35,7 +35,7 @@ EXPORTS = (
     "ppf_surrogate_create", "ppf_surrogate_destroy", "ppf_surrogate_get_config", "ppf_surrogate_num_params",
     "ppf_surrogate_set_params", "ppf_surrogate_get_params", "ppf_surrogate_loss_grad", "ppf_surrogate_train_step",
     "ppf_surrogate_predict", "ppf_surrogate_advance", "ppf_last_error", "ppf_version",
-    "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_last_error",
+    "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_write3d_meta", "ppf_h5_last_error",
 )
 
 _PARAM_FIELDS = ("AS", "AL", "CS", "CL", "cS0", "cL0", "cSeq", "cLeq", "DL", "DS", "sigma", "gamma", "dx", "dt", "l")
@@ -168,6 +168,9 @@ def lib() -> ctypes.CDLL:
         L.ppf_h5_write3d.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
                                      ctypes.POINTER(_dp), ctypes.POINTER(ctypes.c_int64), ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int64)]
+        L.ppf_h5_write3d_meta.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                          ctypes.POINTER(_dp), ctypes.POINTER(ctypes.c_int64), ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_int64), ctypes.c_char_p, _dp, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -477,7 +480,9 @@ def h5_read(path: str, name: str) -> np.ndarray:
     return out
 
 
-def h5_write(path: str, fields: dict, dtype="f64", chunk=None):
+def h5_write(path: str, fields: dict, dtype="f64", chunk=None, meta=None):
+    """Rank-3 datasets of one shape; `meta` = (name, values) adds one float64
+    dataset of shape (1, 1, len(values)) (the program's restart record)."""
     names = list(fields)
     arrs = [_c64(fields[n]) for n in names]
     shape = arrs[0].shape
@@ -487,7 +492,12 @@ def h5_write(path: str, fields: dict, dtype="f64", chunk=None):
     cp = (_dp * len(arrs))(*[a.ctypes.data_as(_dp) for a in arrs])
     dims = (ctypes.c_int64 * 3)(*shape)
     ch = (ctypes.c_int64 * 3)(*chunk) if chunk is not None else None
-    rc = lib().ppf_h5_write3d(path.encode(), len(names), cn, cp, dims, 0 if dtype == "f64" else 1, ch)
+    if meta is None:
+        rc = lib().ppf_h5_write3d(path.encode(), len(names), cn, cp, dims, 0 if dtype == "f64" else 1, ch)
+    else:
+        mv = _c64(np.asarray(meta[1], dtype=np.float64).ravel())
+        rc = lib().ppf_h5_write3d_meta(path.encode(), len(names), cn, cp, dims, 0 if dtype == "f64" else 1, ch,
+                                       meta[0].encode(), mv.ctypes.data_as(_dp), mv.size)
     if rc != 0:
         raise PPFError(rc, lib().ppf_h5_last_error().decode())
 

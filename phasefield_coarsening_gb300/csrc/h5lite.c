@@ -647,30 +647,95 @@ typedef struct {
     uint64_t addr;
 } chunk_ent;
 
+/* object header of one rank-3 float dataset: dataspace, datatype, fill
+ * value, layout (contiguous at `addr` with `bytes`, or chunked with its
+ * B-tree at `addr`); returns the header size */
+static uint64_t ds_header_size(int chunked) { return 16 + (8 + 32) + (8 + 24) + (8 + 8) + (8 + (chunked ? 32 : 24)); }
+
+static void ds_header(uint8_t *buf, const int64_t d[3], int es, const int64_t *chunk, uint64_t addr, uint64_t bytes)
+{
+    const uint64_t sz = ds_header_size(chunk != NULL);
+    memset(buf, 0, sz);
+    buf[0] = 1;
+    put_le(buf + 2, 4, 2);
+    put_le(buf + 4, 1, 4);
+    put_le(buf + 8, sz - 16, 4);
+    size_t p = 16;
+    uint8_t m[64];
+    memset(m, 0, sizeof m);                    /* dataspace v1, rank 3 */
+    m[0] = 1; m[1] = 3;
+    for (int q = 0; q < 3; ++q) put_le(m + 8 + 8 * q, (uint64_t)d[q], 8);
+    p += put_msg(buf + p, 0x0001, 0, m, 32);
+    memset(m, 0, sizeof m);                    /* datatype v1, IEEE float LE */
+    m[0] = 0x11;
+    m[1] = 0x20;                               /* mantissa normalisation: implied MSB */
+    m[2] = (uint8_t)(es * 8 - 1);              /* sign bit position */
+    put_le(m + 4, (uint64_t)es, 4);
+    put_le(m + 8, 0, 2);
+    put_le(m + 10, (uint64_t)es * 8, 2);
+    m[12] = es == 8 ? 52 : 23;                 /* exponent location */
+    m[13] = es == 8 ? 11 : 8;                  /* exponent size */
+    m[14] = 0;                                 /* mantissa location */
+    m[15] = es == 8 ? 52 : 23;                 /* mantissa size */
+    put_le(m + 16, es == 8 ? 1023 : 127, 4);
+    p += put_msg(buf + p, 0x0003, 1, m, 20);
+    memset(m, 0, sizeof m);                    /* fill value v2: early, never, undefined */
+    m[0] = 2; m[1] = 1; m[2] = 2; m[3] = 0;
+    p += put_msg(buf + p, 0x0005, 1, m, 4);
+    memset(m, 0, sizeof m);                    /* layout v3 */
+    m[0] = 3;
+    if (!chunk) {
+        m[1] = 1;
+        put_le(m + 2, addr, 8);
+        put_le(m + 10, bytes, 8);
+        put_msg(buf + p, 0x0008, 0, m, 18);
+    } else {
+        m[1] = 2;
+        m[2] = 4;
+        put_le(m + 3, addr, 8);
+        for (int q = 0; q < 3; ++q) put_le(m + 11 + 4 * q, (uint64_t)chunk[q], 4);
+        put_le(m + 23, (uint64_t)es, 4);
+        put_msg(buf + p, 0x0008, 0, m, 27);
+    }
+}
+
 int ppf_h5_write3d(const char *path, int n, const char *const *names, const double *const *data,
                    const int64_t dims[3], int dtype, const int64_t *chunk)
 {
+    return ppf_h5_write3d_meta(path, n, names, data, dims, dtype, chunk, NULL, NULL, 0);
+}
+
+int ppf_h5_write3d_meta(const char *path, int n, const char *const *names, const double *const *data,
+                        const int64_t dims[3], int dtype, const int64_t *chunk, const char *meta_name,
+                        const double *meta, int nmeta)
+{
     if (!path || !names || !data || !dims || n < 1) return fail(PPF_H5_EARG, "h5: bad argument");
-    if (n > 2 * LEAF_K) return fail(PPF_H5_EARG, "h5: at most %d datasets per file", 2 * LEAF_K);
+    const int has_meta = meta_name != NULL;
+    if (has_meta && (!meta || nmeta < 1 || nmeta > 4096)) return fail(PPF_H5_EARG, "h5: bad metadata");
+    const int nt = n + has_meta;                   /* datasets in the file: fields, then the metadata */
+    const char *all[2 * LEAF_K + 1];
+    if (nt > 2 * LEAF_K) return fail(PPF_H5_EARG, "h5: at most %d datasets per file", 2 * LEAF_K);
+    for (int i = 0; i < n; ++i) all[i] = names[i];
+    if (has_meta) all[n] = meta_name;
     if (dtype != PPF_H5_F64 && dtype != PPF_H5_F32) return fail(PPF_H5_EARG, "h5: bad dtype");
     for (int i = 0; i < 3; ++i) {
         if (dims[i] <= 0) return fail(PPF_H5_EDIMS, "h5: bad dims");
         if (chunk && (chunk[i] <= 0 || chunk[i] > dims[i])) return fail(PPF_H5_EDIMS, "h5: bad chunk dims");
     }
-    for (int i = 0; i < n; ++i) {
-        if (!names[i] || !names[i][0] || strlen(names[i]) > 255 || strchr(names[i], '/'))
+    for (int i = 0; i < nt; ++i) {
+        if (!all[i] || !all[i][0] || strlen(all[i]) > 255 || strchr(all[i], '/'))
             return fail(PPF_H5_EARG, "h5: bad dataset name");
         for (int j = 0; j < i; ++j)
-            if (strcmp(names[i], names[j]) == 0) return fail(PPF_H5_EARG, "h5: duplicate dataset name");
+            if (strcmp(all[i], all[j]) == 0) return fail(PPF_H5_EARG, "h5: duplicate dataset name");
     }
     const int es = dtype == PPF_H5_F64 ? 8 : 4;
     const int64_t nel = dims[0] * dims[1] * dims[2];
 
     /* sorted order of names (symbol nodes must be sorted by name) */
     int order[2 * LEAF_K];
-    for (int i = 0; i < n; ++i) order[i] = i;
-    for (int i = 1; i < n; ++i)
-        for (int j = i; j > 0 && strcmp(names[order[j - 1]], names[order[j]]) > 0; --j) {
+    for (int i = 0; i < nt; ++i) order[i] = i;
+    for (int i = 1; i < nt; ++i)
+        for (int j = i; j > 0 && strcmp(all[order[j - 1]], all[order[j]]) > 0; --j) {
             int t = order[j]; order[j] = order[j - 1]; order[j - 1] = t;
         }
 
@@ -681,17 +746,18 @@ int ppf_h5_write3d(const char *path, int n, const char *const *names, const doub
     const uint64_t A_HEAPDATA = A_HEAP + 32;
     uint64_t name_off[2 * LEAF_K];
     uint64_t hs = 8;                                    /* offset 0: the empty name */
-    for (int s = 0; s < n; ++s) { name_off[order[s]] = hs; hs += round8(strlen(names[order[s]]) + 1); }
+    for (int s = 0; s < nt; ++s) { name_off[order[s]] = hs; hs += round8(strlen(all[order[s]]) + 1); }
     const uint64_t A_BTREE = A_HEAPDATA + hs;
     const uint64_t BTREE_SZ = 24 + (2 * GROUP_K + 1) * 8 + 2 * GROUP_K * 8;
     const uint64_t A_SNOD = A_BTREE + BTREE_SZ;
     const uint64_t SNOD_SZ = 8 + 2 * LEAF_K * 40;
 
     /* dataset object header: dataspace 32, datatype 24, fill 8, layout 24|32 (+8 each header) */
-    const uint64_t DS_SZ = 16 + (8 + 32) + (8 + 24) + (8 + 8) + (8 + (chunk ? 32 : 24));
+    const uint64_t DS_SZ = ds_header_size(chunk != NULL);
     uint64_t a_ds[2 * LEAF_K];
     uint64_t pos = A_SNOD + SNOD_SZ;
     for (int i = 0; i < n; ++i) { a_ds[i] = pos; pos += DS_SZ; }
+    if (has_meta) { a_ds[n] = pos; pos += ds_header_size(0); }
 
     /* chunk index plan */
     int64_t ncd[3] = {1, 1, 1}, nchunks = 1, csz = 0;
@@ -719,6 +785,8 @@ int ppf_h5_write3d(const char *path, int n, const char *const *names, const doub
         a_data[i] = pos;
         pos += chunk ? (uint64_t)(nchunks * csz) : (uint64_t)(nel * es);
     }
+    uint64_t a_meta = 0;
+    if (has_meta) { a_meta = pos; pos += (uint64_t)nmeta * 8; }
     const uint64_t eof = pos;
 
     FILE *f = fopen(path, "wb");
@@ -769,7 +837,7 @@ int ppf_h5_write3d(const char *path, int n, const char *const *names, const doub
     }
     if (!rc) {
         memset(buf, 0, hs);
-        for (int i = 0; i < n; ++i) memcpy(buf + name_off[i], names[i], strlen(names[i]));
+        for (int i = 0; i < nt; ++i) memcpy(buf + name_off[i], all[i], strlen(all[i]));
         rc = wr_bytes(f, &w, buf, hs);
     }
     /* ---- group B-tree: one leaf pointing at one symbol node ---- */
@@ -783,7 +851,7 @@ int ppf_h5_write3d(const char *path, int n, const char *const *names, const doub
         put_le(buf + 16, UNDEF_ADDR, 8);
         put_le(buf + 24, 0, 8);                        /* key 0: "" */
         put_le(buf + 32, A_SNOD, 8);                   /* child 0 */
-        put_le(buf + 40, name_off[order[n - 1]], 8);   /* key 1: largest name */
+        put_le(buf + 40, name_off[order[nt - 1]], 8);  /* key 1: largest name */
         rc = wr_bytes(f, &w, buf, BTREE_SZ);
     }
     /* ---- symbol table node ---- */
@@ -791,8 +859,8 @@ int ppf_h5_write3d(const char *path, int n, const char *const *names, const doub
         memset(buf, 0, SNOD_SZ);
         memcpy(buf, "SNOD", 4);
         buf[4] = 1;
-        put_le(buf + 6, (uint64_t)n, 2);
-        for (int s = 0; s < n; ++s) {
+        put_le(buf + 6, (uint64_t)nt, 2);
+        for (int s = 0; s < nt; ++s) {
             uint8_t *e = buf + 8 + 40 * s;
             put_le(e, name_off[order[s]], 8);
             put_le(e + 8, a_ds[order[s]], 8);
@@ -801,49 +869,13 @@ int ppf_h5_write3d(const char *path, int n, const char *const *names, const doub
     }
     /* ---- dataset object headers ---- */
     for (int i = 0; i < n && !rc; ++i) {
-        memset(buf, 0, DS_SZ);
-        buf[0] = 1;
-        put_le(buf + 2, 4, 2);
-        put_le(buf + 4, 1, 4);
-        put_le(buf + 8, DS_SZ - 16, 4);
-        size_t p = 16;
-        uint8_t m[64];
-        memset(m, 0, sizeof m);                    /* dataspace v1, rank 3 */
-        m[0] = 1; m[1] = 3;
-        for (int q = 0; q < 3; ++q) put_le(m + 8 + 8 * q, (uint64_t)dims[q], 8);
-        p += put_msg(buf + p, 0x0001, 0, m, 32);
-        memset(m, 0, sizeof m);                    /* datatype v1, IEEE float LE */
-        m[0] = 0x11;
-        m[1] = 0x20;                               /* mantissa normalisation: implied MSB */
-        m[2] = (uint8_t)(es * 8 - 1);              /* sign bit position */
-        put_le(m + 4, (uint64_t)es, 4);
-        put_le(m + 8, 0, 2);
-        put_le(m + 10, (uint64_t)es * 8, 2);
-        m[12] = es == 8 ? 52 : 23;                 /* exponent location */
-        m[13] = es == 8 ? 11 : 8;                  /* exponent size */
-        m[14] = 0;                                 /* mantissa location */
-        m[15] = es == 8 ? 52 : 23;                 /* mantissa size */
-        put_le(m + 16, es == 8 ? 1023 : 127, 4);
-        p += put_msg(buf + p, 0x0003, 1, m, 20);
-        memset(m, 0, sizeof m);                    /* fill value v2: early, never, undefined */
-        m[0] = 2; m[1] = 1; m[2] = 2; m[3] = 0;
-        p += put_msg(buf + p, 0x0005, 1, m, 4);
-        memset(m, 0, sizeof m);                    /* layout v3 */
-        m[0] = 3;
-        if (!chunk) {
-            m[1] = 1;
-            put_le(m + 2, a_data[i], 8);
-            put_le(m + 10, (uint64_t)(nel * es), 8);
-            p += put_msg(buf + p, 0x0008, 0, m, 18);
-        } else {
-            m[1] = 2;
-            m[2] = 4;
-            put_le(m + 3, a_idx[i], 8);
-            for (int q = 0; q < 3; ++q) put_le(m + 11 + 4 * q, (uint64_t)chunk[q], 4);
-            put_le(m + 23, (uint64_t)es, 4);
-            p += put_msg(buf + p, 0x0008, 0, m, 27);
-        }
+        ds_header(buf, dims, es, chunk, chunk ? a_idx[i] : a_data[i], (uint64_t)(nel * es));
         rc = wr_bytes(f, &w, buf, DS_SZ);
+    }
+    if (has_meta && !rc) {
+        const int64_t md[3] = {1, 1, nmeta};
+        ds_header(buf, md, 8, NULL, a_meta, (uint64_t)nmeta * 8);
+        rc = wr_bytes(f, &w, buf, ds_header_size(0));
     }
     /* ---- chunk B-trees (one per dataset, levels bottom-up) ---- */
     if (chunk && !rc) {
@@ -953,6 +985,10 @@ int ppf_h5_write3d(const char *path, int n, const char *const *names, const doub
         }
     }
     free(tmp);
+    if (has_meta && !rc) {
+        if (w != a_meta) rc = fail(PPF_H5_EIO, "h5: internal layout error");
+        else rc = wr_bytes(f, &w, meta, (uint64_t)nmeta * 8);
+    }
     if (!rc && w != eof) rc = fail(PPF_H5_EIO, "h5: internal size error");
     if (fclose(f) != 0 && !rc) rc = fail(PPF_H5_EIO, "h5: close failed");
     if (rc) remove(path);

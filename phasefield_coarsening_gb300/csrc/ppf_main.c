@@ -35,6 +35,14 @@
  *                          /etaL read goes through the closed /etaS
  *                          identifier (:1032) and leaves etaL = 1.0
  *   --timing               print step throughput on stderr at the end
+ *   --restart              continue the run a saved file belongs to: every
+ *                          file written holds a dataset /ppf_restart =
+ *                          (next iteration, dt, save number, error); with
+ *                          --restart the loop resumes there (same save
+ *                          iterations, numbering continued from that save,
+ *                          same convergence test, dt from the file unless
+ *                          --dt is given), so a restarted run writes what
+ *                          the uninterrupted run would have written
  */
 #define _POSIX_C_SOURCE 200809L
 #include <math.h>
@@ -78,7 +86,7 @@ int main(int argc, char **argv)
         return -1;
     }
     const char *input = argv[1];
-    int bc = PPF_BC_NOFLUX, prec = PPF_F64, etaL_bug = 0, timing = 0;
+    int bc = PPF_BC_NOFLUX, prec = PPF_F64, etaL_bug = 0, timing = 0, restart = 0, dt_given = 0;
     int64_t n_iter = 5000001L, n_save = 50000L, n_iter_init = 100000000L;
     double threshold = 1.0e-12, dt = 0.0;
     int64_t chunk[3] = {0, 0, 0};
@@ -93,7 +101,7 @@ int main(int argc, char **argv)
         } else if (!strcmp(o, "--steps") && more) n_iter = strtoll(argv[++a], NULL, 10);
         else if (!strcmp(o, "--save") && more) n_save = strtoll(argv[++a], NULL, 10);
         else if (!strcmp(o, "--init") && more) n_iter_init = strtoll(argv[++a], NULL, 10);
-        else if (!strcmp(o, "--dt") && more) dt = strtod(argv[++a], NULL);
+        else if (!strcmp(o, "--dt") && more) { dt = strtod(argv[++a], NULL); dt_given = 1; }
         else if (!strcmp(o, "--threshold") && more) threshold = strtod(argv[++a], NULL);
         else if (!strcmp(o, "--precision") && more) {
             const char *v = argv[++a];
@@ -104,6 +112,7 @@ int main(int argc, char **argv)
             for (int q = 0; q < 3; ++q) chunk[q] = strtoll(argv[++a], NULL, 10);
         } else if (!strcmp(o, "--ref-etaL-bug")) etaL_bug = 1;
         else if (!strcmp(o, "--timing")) timing = 1;
+        else if (!strcmp(o, "--restart")) restart = 1;
         else {
             fprintf(STD_BUF, "Usage:\nppf filename\n");
             return -1;
@@ -138,18 +147,37 @@ int main(int argc, char **argv)
     if (ppf_h5_read3d(input, "/c", d2, c, n) != 0) return die(input, ppf_h5_last_error());
     if (memcmp(d2, dims, sizeof dims)) return die(input, "/c and /etaS differ in size");
 
+    /* restart record written with every save (see --restart) */
+    int64_t i_start = 0;
+    int save_start = 0;
+    double error_start = threshold;
+    if (restart) {
+        int64_t rd[3];
+        double rec[4];
+        if (ppf_h5_dims(input, "/ppf_restart", rd) != 0) return die(input, "no /ppf_restart record to restart from");
+        if (rd[0] != 1 || rd[1] != 1 || rd[2] != 4 || ppf_h5_read3d(input, "/ppf_restart", rd, rec, 4) != 0)
+            return die(input, "malformed /ppf_restart record");
+        if (!(rec[0] >= 0) || !(rec[1] > 0) || !(rec[2] >= 0)) return die(input, "malformed /ppf_restart record");
+        i_start = (int64_t)rec[0];
+        save_start = (int)rec[2];
+        error_start = rec[3];
+        if (!dt_given) dt = rec[1];
+    }
+
     ppf_params prm;
     ppf_params_default(&prm);
     prm.dt = dt;
+    ppf_derived der;
+    if (ppf_params_derive(&prm, &der) != 0) return die("parameters", ppf_last_error());
     ppf_ctx *ctx = NULL;
     if (ppf_create((int)dims[0], (int)dims[1], (int)dims[2], &prm, bc, prec, &ctx) != 0)
         return die("device", ppf_last_error());
     if (ppf_upload(ctx, etaS, etaL, c) != 0) return die("upload", ppf_last_error());
 
     /* main loop, :178-258 */
-    int64_t i_iter = 0;
-    double error = threshold;
-    int save_iter = 0;
+    int64_t i_iter = i_start;
+    double error = error_start;
+    int save_iter = save_start;
     double t_steps = 0.0;
     int64_t n_steps = 0;
     char *fname = (char *)malloc(len + 32);
@@ -178,7 +206,9 @@ int main(int argc, char **argv)
         if (ppf_download(ctx, etaS, etaL, c) != 0) return die("download", ppf_last_error());
         const char *names[3] = {"etaS", "etaL", "c"};
         const double *data[3] = {etaS, etaL, c};
-        if (ppf_h5_write3d(fname, 3, names, data, dims, PPF_H5_F64, chunk[0] > 0 ? chunk : NULL) != 0)
+        const double rec[4] = {(double)i_iter, der.dt, (double)save_iter, error};
+        if (ppf_h5_write3d_meta(fname, 3, names, data, dims, PPF_H5_F64, chunk[0] > 0 ? chunk : NULL, "ppf_restart",
+                                rec, 4) != 0)
             return die(fname, ppf_h5_last_error());
     }
     if (timing && t_steps > 0)

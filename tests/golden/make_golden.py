@@ -9,7 +9,7 @@ written with the project's HDF5 writer, and its output file and its stderr
 convergence line are stored next to the input in one .npz.
 
 Run from the repository root (needs the reference sources):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case names]
 """
 from __future__ import annotations
 
@@ -57,14 +57,20 @@ CASES = {
     "noflux_conly_6x6x6": ((6, 6, 6), 1, 16, 15, 10, None, True, 4),
     "periodic_dt08_8x8x8": ((8, 8, 8), 0, 41, 40, None, "0.8*dx*dx/(6.0*DL)", True, 5),
     "etaL_bug_6x7x8": ((6, 7, 8), 0, 11, 10, None, None, False, 6),
+    # uniform liquid: every increment is zero, so the convergence test
+    # (err < 1e-12 at a save, phasefield.c:247-250) stops the run at the first save
+    "converged_uniform_6x6x6": ((6, 6, 6), 0, 51, 10, None, None, True, 7, "uniform"),
 }
 
 
 def make_case(name, spec, work):
-    shape, bc, n_iter, n_save, n_init, dt_expr, fix, seed = spec
+    shape, bc, n_iter, n_save, n_init, dt_expr, fix, seed = spec[:8]
     from phasefield_coarsening_gb300 import write_fields, read_fields
     rng = np.random.default_rng(seed)
-    etaS, etaL, c = smooth_random(shape, rng)
+    if len(spec) > 8 and spec[8] == "uniform":
+        etaS, etaL, c = np.zeros(shape), np.ones(shape), np.full(shape, 0.95)
+    else:
+        etaS, etaL, c = smooth_random(shape, rng)
     inp = os.path.join(work, f"{name}.h5")
     write_fields(inp, etaS, etaL, c)
     exe = build_ref.build(*shape, bc=bc, n_iter=n_iter, n_save=n_save, n_iter_init=n_init, dt_expr=dt_expr,
@@ -79,7 +85,7 @@ def make_case(name, spec, work):
                       float(m.group(6))])
     arrays = {"in_etaS": etaS, "in_etaL": etaL, "in_c": c, "saves": np.array(saves)}
     for k, fn in enumerate(outs):
-        oS, oL, oc = read_fields(fn)
+        oS, oL, oc = read_fields(fn if os.path.isabs(fn) else os.path.join(work, fn))
         arrays[f"out{k + 1}_etaS"], arrays[f"out{k + 1}_etaL"], arrays[f"out{k + 1}_c"] = oS, oL, oc
     meta = dict(shape=list(shape), bc=bc, n_iter=n_iter, n_save=n_save,
                 n_iter_init=n_init if n_init is not None else 100000000, dt_expr=dt_expr or "0.125*dx*dx/DL",
@@ -94,6 +100,8 @@ if __name__ == "__main__":
     work = tempfile.mkdtemp(prefix="ppf_golden_")
     try:
         for name, spec in CASES.items():
+            if len(sys.argv) > 1 and name not in sys.argv[1:]:
+                continue
             meta = make_case(name, spec, work)
             print(name, meta["outputs"])
     finally:

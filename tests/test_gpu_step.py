@@ -209,7 +209,8 @@ def test_state_errors():
             s.upload(np.zeros((4, 4, 5)), np.zeros((4, 4, 4)), np.zeros((4, 4, 4)))
 
 
-@pytest.mark.parametrize("name", ["periodic_8x10x12", "noflux_conly_6x6x6", "etaL_bug_6x7x8"])
+@pytest.mark.parametrize("name", ["periodic_8x10x12", "noflux_conly_6x6x6", "etaL_bug_6x7x8",
+                                  "converged_uniform_6x6x6"])
 def test_ppf_program_matches_reference_run(name, tmp_path):
     """The `ppf` program on the reference's own input: same output files,
     same convergence lines (phasefield.c:240, :248, :267)."""
@@ -232,9 +233,11 @@ def test_ppf_program_matches_reference_run(name, tmp_path):
         got = ppf.read_fields(fn)
         for f, arr in zip(("etaS", "etaL", "c"), got):
             assert maxabs(arr, d[f"out{k + 1}_{f}"]) <= 1e-12
-    # identical text up to the last printed digit (sums agree to ~1e-14)
+    # identical text up to the last printed digit (sums agree to ~1e-14); the
+    # stop (after n_iter, or at the first save with err < threshold) at the same step
     for a, b in zip(my_lines, ref_lines):
         assert a.split("\t")[0].split(":")[0] == b.split("\t")[0].split(":")[0]
+    assert my_lines[-1].split(";")[0] == ref_lines[-1].split(";")[0]
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
@@ -275,3 +278,32 @@ def test_autotune_keeps_state_and_picks_a_valid_choice():
         got = s.download()
     ref = oracle.run(*st, 7, bc=0)
     assert max(float(np.abs(a - b).max()) for a, b in zip(got, ref[:3])) <= 1e-5
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_ppf_restart_continues_the_run_exactly(precision, tmp_path):
+    """A run restarted from one of its own output files (--restart reads the
+    /ppf_restart record: next iteration, dt, save number, error) writes the
+    same later files, bit for bit, and the same convergence lines."""
+    shape = (8, 10, 12)
+    inp = str(tmp_path / "job.h5")
+    ppf.write_fields(inp, *smooth_state(shape, seed=31))
+    opts = ["--bc", "periodic", "--steps", "35", "--save", "10", "--dt", repr(DT08), "--precision", precision]
+    r = subprocess.run([ppf.EXE_PATH, inp] + opts, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    outs = [ln for ln in r.stdout.splitlines() if ln]
+    assert [os.path.basename(o) for o in outs] == ["job_1.h5", "job_2.h5", "job_3.h5"]
+    rec = ppf.h5_read(outs[0], "ppf_restart").ravel()
+    assert rec[0] == 11 and rec[1] == DT08 and rec[2] == 1
+    # restart from the first save, dt taken from the record
+    opts_r = [o for o in opts if o not in ("--dt", repr(DT08))] + ["--restart"]
+    r2 = subprocess.run([ppf.EXE_PATH, outs[0]] + opts_r, capture_output=True, text=True, timeout=120)
+    assert r2.returncode == 0, r2.stderr
+    outs2 = [ln for ln in r2.stdout.splitlines() if ln]
+    assert [os.path.basename(o) for o in outs2] == ["job_1_2.h5", "job_1_3.h5"]
+    for a, b in zip(outs[1:], outs2):
+        for x, y in zip(ppf.read_fields(a), ppf.read_fields(b)):
+            assert np.array_equal(x, y)
+        assert np.array_equal(ppf.h5_read(a, "ppf_restart"), ppf.h5_read(b, "ppf_restart"))
+    conv = lambda t: [ln for ln in t.splitlines() if ": c=" in ln or ln.startswith("Total steps")]
+    assert conv(r.stderr)[1:] == conv(r2.stderr)

@@ -115,3 +115,18 @@ def test_user_block_is_skipped(tmp_path):
     ub = tmp_path / "ub.h5"
     ub.write_bytes(b"\0" * 512 + raw)
     assert np.array_equal(ppf.h5_read(str(ub), "etaS"), f["etaS"])
+
+
+def test_metadata_dataset_round_trip(tmp_path):
+    """The restart record: a (1, 1, n) float64 dataset next to the fields,
+    found by name, leaving the fields as they were (contiguous and chunked)."""
+    rng = np.random.default_rng(5)
+    f = {k: rng.random((4, 5, 6)) for k in ("etaS", "etaL", "c")}
+    rec = [123.0, 1.25e13, 7.0, 3.5e-9]
+    for chunk in (None, (2, 5, 3)):
+        p = str(tmp_path / f"m{chunk is None}.h5")
+        ppf.h5_write(p, f, chunk=chunk, meta=("ppf_restart", rec))
+        assert ppf.h5_dims(p, "ppf_restart") == (1, 1, 4)
+        assert np.array_equal(ppf.h5_read(p, "ppf_restart").ravel(), rec)
+        for k, v in f.items():
+            assert np.array_equal(ppf.h5_read(p, k), v)

@@ -51,6 +51,25 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value: float) -> float:
+    """The largest of one float per rank (the job's time is its slowest
+    rank's); the value itself when not running under torch.distributed."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_glups(world: int, cells: int, time_steps: int, seconds: float) -> float:
+    """Whole-job lattice updates per second (replicas: every rank advances
+    its own `cells`-cell domain by `time_steps`)."""
+    return world * cells * time_steps / seconds / 1e9
+
+
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -259,11 +278,8 @@ def run_ours(args):
     clk = clocks.stop()
     total_ms = t0.elapsed_time(t1)
     step_ms = sum(a.elapsed_time(b) for a, b in ev) / (args.steps * INNER)   # per f32 step launch
-    if world > 1:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
-    value = world * cells * INNER * args.steps / (total_ms * 1e-3) / 1e9
+    total_ms = max_over_ranks(total_ms)
+    value = job_glups(world, cells, INNER * args.steps, total_ms * 1e-3)
 
     # e2e through the C-ABI with pinned host buffers
     host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (eS, eL, c)]
@@ -286,11 +302,8 @@ def run_ours(args):
         e2e_step()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - w0
-    if world > 1:
-        tt = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e_value = world * cells * INNER * args.steps / e2e_s / 1e9
+    e2e_s = max_over_ranks(e2e_s)
+    e2e_value = job_glups(world, cells, INNER * args.steps, e2e_s)
 
     if rank == 0:
         hbm, src = peaks()
@@ -341,6 +354,9 @@ def run_ensemble(args):
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     doms = ic.ensemble_workload(seed=args.seed + rank)
     shapes = [d[0].shape for d in doms]
     cells = int(sum(np.prod(s) for s in shapes))
@@ -364,9 +380,9 @@ def run_ensemble(args):
 
     clocks = ClockSampler(local)
     clocks.start()
-    ens_s = timed(lambda: ens.step(INNER), ens.sync)
+    ens_s = max_over_ranks(timed(lambda: ens.step(INNER), ens.sync))
     clk = clocks.stop()
-    value = cells * INNER * args.steps / ens_s / 1e9
+    value = job_glups(world, cells, INNER * args.steps, ens_s)
 
     sims = []
     for eS, eL, c, _ in doms:
@@ -379,8 +395,8 @@ def run_ensemble(args):
         for s in sims:
             s.step(INNER)
 
-    seq_s = timed(seq_step, lambda: [s.sync() for s in sims])
-    seq_value = cells * INNER * args.steps / seq_s / 1e9
+    seq_s = max_over_ranks(timed(seq_step, lambda: [s.sync() for s in sims]))
+    seq_value = job_glups(world, cells, INNER * args.steps, seq_s)
     # bit-exact agreement of the two paths on one domain after equal step counts
     same = all(np.array_equal(a, b) for a, b in zip(ens.download(0), sims[0].download()))
     for s in sims:
@@ -393,8 +409,8 @@ def run_ensemble(args):
         for i in range(len(doms)):
             ens.download(i)
 
-    e2e_s = timed(e2e_step, ens.sync)
-    e2e_value = cells * INNER * args.steps / e2e_s / 1e9
+    e2e_s = max_over_ranks(timed(e2e_step, ens.sync))
+    e2e_value = job_glups(world, cells, INNER * args.steps, e2e_s)
     if rank == 0:
         line = {
             "metric": "GLUPS (ensemble of 64 domains, one persistent launch per time step)", "value": round(value, 3),
@@ -416,6 +432,8 @@ def run_ensemble(args):
         }
         print(json.dumps(line), flush=True)
     ens.close()
+    if world > 1:
+        dist.destroy_process_group()
 
 
 def run_reference(args):

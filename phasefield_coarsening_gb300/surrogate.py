@@ -246,8 +246,27 @@ if __name__ == "__main__":
     ap.add_argument("--k", type=int, default=50)
     ap.add_argument("--iters", type=int, default=2000)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--out", required=True)
+    ap.add_argument("--out")
+    ap.add_argument("--profile-call", type=int, metavar="EDGE",
+                    help="instead of training: one surrogate call on an EDGE^3 FP32 state (a fixed launch "
+                         "sequence to capture with a profiler: features, 6 convolutions, mass projection)")
     a = ap.parse_args()
+    if a.profile_call:
+        n = a.profile_call
+        z, y, x = np.meshgrid(*[np.arange(n)] * 3, indexing="ij")
+        eS = 0.5 * (1 + np.tanh(3 * np.sin(2 * np.pi * x / n * 4) * np.cos(2 * np.pi * y / n * 4) *
+                                np.sin(2 * np.pi * z / n * 4)))
+        st = (eS, 1.0 - eS, 0.476 * eS + 0.999 * (1 - eS))
+        sim = Simulation((n, n, n), params_default(dt=DT), "periodic", "f32")
+        sim.upload(*st)
+        net = Surrogate(width=a.width, k_steps=a.k)
+        net.set_params(init_params(a.width, seed=a.seed))
+        net.advance(sim, 1)
+        sim.sync()
+        print(json.dumps({"profile_call": n, "width": a.width, "ok": True}))
+        raise SystemExit(0)
+    if not a.out:
+        ap.error("--out is required for training")
     t0 = time.time()
     net, log = fit(width=a.width, k=a.k, iters=a.iters, seed=a.seed)
     save(net, a.out, iters=a.iters, seed=a.seed, train_s=round(time.time() - t0, 1), log=log)

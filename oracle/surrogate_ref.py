@@ -2,7 +2,8 @@
 
 CPU restatement (numpy) of the surrogate network that
 phasefield_coarsening_gb300/csrc/ppf_surrogate.cu and ppf_nn_conv.cu run on
-the GPU: features, six periodic 3x3x3 convolutions with SiLU, the residual
+the GPU: features, six 3x3x3 convolutions (periodic halos, or mirrored no-flux
+halos for inference) with SiLU, the residual
 output, the squared-error loss against a stencil target, and the full
 backward pass.  The reference has no learned component; the network stands
 in for k_steps calls of its explicit step (phasefield.c:301-403), whose own
@@ -82,11 +83,20 @@ def taps():
                 yield (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1), dz, dy, dx
 
 
-def conv(x, W):
-    """y[co, v] = sum_tap W[tap] @ x[:, v + d(tap)], periodic; x (ci, z, y, x)."""
+def conv(x, W, bc="periodic"):
+    """y[co, v] = sum_tap W[tap] @ x[:, v + d(tap)]; x (ci, z, y, x).  Halo:
+    periodic images, or for "noflux" the mirror of the reference's no-flux
+    fill (ghost -1 = cell 0, ghost n = cell n-1, phasefield.c:1151-1189)."""
     y = np.zeros((W.shape[1],) + x.shape[1:])
+    if bc == "periodic":
+        for t, dz, dy, dx in taps():
+            xs = np.roll(x, shift=(-dz, -dy, -dx), axis=(1, 2, 3))
+            y += np.einsum("oc,czyx->ozyx", W[t], xs, optimize=True)
+        return y
+    xp = np.pad(x, ((0, 0), (1, 1), (1, 1), (1, 1)), mode="edge")
+    nz, ny, nx = x.shape[1:]
     for t, dz, dy, dx in taps():
-        xs = np.roll(x, shift=(-dz, -dy, -dx), axis=(1, 2, 3))
+        xs = xp[:, 1 + dz:1 + dz + nz, 1 + dy:1 + dy + ny, 1 + dx:1 + dx + nx]
         y += np.einsum("oc,czyx->ozyx", W[t], xs, optimize=True)
     return y
 
@@ -132,7 +142,7 @@ def features(eS, eL, c, cfg):
     return f
 
 
-def forward(state, params, cfg, rounding="device"):
+def forward(state, params, cfg, rounding="device", bc="periodic"):
     """Network output (3 channels, in units of out_scale) and the tape."""
     r = bf16 if rounding == "device" else (lambda a: np.asarray(a, np.float64))
     layers = unflatten(params, cfg["width"])
@@ -140,12 +150,12 @@ def forward(state, params, cfg, rounding="device"):
     tape = {"a": [a], "z": []}
     for li in range(LAYERS - 1):
         W, b = layers[li]
-        h = conv(a, r(W)) + b[:, None, None, None]
+        h = conv(a, r(W), bc) + b[:, None, None, None]
         tape["z"].append(r(h))
         a = r(silu(h))
         tape["a"].append(a)
     W, b = layers[-1]
-    out = conv(a, r(W)) + b[:, None, None, None]
+    out = conv(a, r(W), bc) + b[:, None, None, None]
     return out[:3], tape
 
 

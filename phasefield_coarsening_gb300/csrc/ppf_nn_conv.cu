@@ -247,8 +247,10 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                 const Item w = item_of(g, a.yc, it);
                 for (int r = w.y0 - 1; r <= w.y1; ++r, ++q) {
                     const uint32_t s = q % C::RING;
+                    // the producer runs ahead of the MMAs: its waits for a free slot
+                    // sleep between polls instead of taking issue slots
                     if (q >= (uint32_t)C::RING &&
-                        !wait_or_abort(empty(s), ((q / C::RING) + 1) & 1, a.limit_ns, abort_flag)) {
+                        !wait_backoff(empty(s), ((q / C::RING) + 1) & 1, a.limit_ns, abort_flag)) {
                         fail(abort_flag, a.err, 1);
                         ok = false;
                         break;
@@ -598,7 +600,7 @@ __global__ void __launch_bounds__(192, 1) wgrad_kernel(const WgradArgs a) {
             for (int tt = t0; tt < t1; ++tt, ++n) {
                 const uint32_t st = n % C::NST;
                 if (n >= (uint32_t)C::NST &&
-                    !wait_or_abort(empty(st), ((n / C::NST) + 1) & 1, a.limit_ns, abort_flag)) {
+                    !wait_backoff(empty(st), ((n / C::NST) + 1) & 1, a.limit_ns, abort_flag)) {
                     fail(abort_flag, a.err, 1);
                     break;
                 }

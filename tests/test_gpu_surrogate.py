@@ -44,6 +44,27 @@ def test_forward_matches_oracle(width, shape):
     assert np.linalg.norm(got - ref) <= 5e-3 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("width", [16, 32])
+def test_forward_on_noflux_domain_matches_oracle(width):
+    """Inference on a no-flux domain: every activation's halo holds the
+    mirror images (ghost -1 = cell 0, ghost n = cell n-1)."""
+    shape = (5, 6, 128)
+    state = smooth_state(shape, seed=17)
+    p = sr.init_params(width, seed=8, last_scale=1.0)
+    with ppf.Surrogate(width=width) as net, make_sim(shape, state, bc="noflux") as sim:
+        net.set_params(p)
+        got = net.predict(sim)
+        cfg = net.config
+    pred, _ = sr.forward(state, p, cfg, bc="noflux")
+    ref = pred * np.asarray(cfg["out_scale"])[:, None, None, None]
+    assert np.abs(got - ref).max() <= 2e-2 * np.abs(ref).max()
+    assert np.linalg.norm(got - ref) <= 5e-3 * np.linalg.norm(ref)
+    # and it is not the periodic answer
+    per, _ = sr.forward(state, p, cfg)
+    per = per * np.asarray(cfg["out_scale"])[:, None, None, None]
+    assert np.linalg.norm(per - ref) > 20 * np.linalg.norm(got - ref)
+
+
 @pytest.mark.parametrize("width", [32, 16])
 def test_loss_and_gradients_match_oracle(width):
     shape = (4, 6, 128)

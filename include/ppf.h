@@ -265,8 +265,10 @@ int ppf_copy_state(ppf_ctx *dst, ppf_ctx *src);
  *   state += out_scale * net(etaS, etaL, (c - c_eq(h)) * in_scale_c)
  * followed by the FP64 mass projection back to the pre-call sum(c).
  * Trained on the device on (state, state after k_steps stencil steps)
- * pairs.  Domains: FP32 contexts whose x edge is a multiple of 128;
- * training on periodic domains. */
+ * pairs.  Domains: FP32 contexts whose x edge is a multiple of 128 and
+ * whose y and z edges are at least 2; training on periodic domains.  A
+ * surrogate keeps one workspace (for the last domain shape it ran on) and
+ * is used by one host thread at a time. */
 typedef struct ppf_surrogate ppf_surrogate;
 
 typedef struct {

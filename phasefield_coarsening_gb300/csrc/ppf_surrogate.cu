@@ -247,11 +247,10 @@ struct ppf_surrogate {
     int wz = 0, wy = 0, wx = 0, wbc = -1;
     NNGeom g{};
     uint16_t *feat = nullptr, *act[5] = {}, *zp[5] = {}, *g16 = nullptr, *gw[2] = {};
+    bool train_ready = false;    // g16, gw, zp allocated for the current shape
     float *wpart = nullptr, *bpart = nullptr;
     double *mpart = nullptr;     // per-CTA sums of c after a call (output layer)
     double *dscal = nullptr;     // [0] loss
-    double *dpart = nullptr;
-    int dpart_cap = 0;
     float *scratch = nullptr;    // predictions: zero state + output state
     double *stage = nullptr;
     size_t scratch_elems = 0;
@@ -260,15 +259,24 @@ struct ppf_surrogate {
 
 namespace {
 
-void free_ws(ppf_surrogate *s) {
-    cudaFree(s->feat);
-    for (auto &p : s->act) cudaFree(p), p = nullptr;
+void free_train(ppf_surrogate *s) {
     for (auto &p : s->zp) cudaFree(p), p = nullptr;
     for (auto &p : s->gw) cudaFree(p), p = nullptr;
     cudaFree(s->g16);
+    s->g16 = nullptr;
+    s->train_ready = false;
+}
+
+// buffers may still be in use by work queued on any context's stream: the
+// whole device is synchronised before anything is freed
+void free_ws(ppf_surrogate *s) {
+    cudaDeviceSynchronize();
+    free_train(s);
+    cudaFree(s->feat);
+    for (auto &p : s->act) cudaFree(p), p = nullptr;
     cudaFree(s->scratch);
     cudaFree(s->stage);
-    s->feat = s->g16 = nullptr;
+    s->feat = nullptr;
     s->scratch = nullptr;
     s->stage = nullptr;
     s->scratch_elems = 0;
@@ -296,7 +304,6 @@ int ensure_ws(ppf_surrogate *s, ppf_ctx *c, bool train) {
     if (rc) return rc;
     if (c->dev != s->dev) return serr(PPF_EINVAL, "context and surrogate on different devices");
     if (s->wz != c->nz || s->wy != c->ny || s->wx != c->nx || s->wbc != c->bc) {
-        SCU(cudaStreamSynchronize(c->stream));
         free_ws(s);
         s->g = make_nngeom(c->nz, c->ny, c->nx, c->bc);
         if ((rc = alloc_zero((void **)&s->feat, act_bytes(s->g, 16), c->stream))) return rc;
@@ -307,12 +314,19 @@ int ensure_ws(ppf_surrogate *s, ppf_ctx *c, bool train) {
         s->wx = c->nx;
         s->wbc = c->bc;
     }
-    if (train && !s->g16) {
-        if ((rc = alloc_zero((void **)&s->g16, act_bytes(s->g, 16), c->stream))) return rc;
+    if (train && !s->train_ready) {
+        // all or nothing: a failure leaves no half-allocated training set
+        rc = alloc_zero((void **)&s->g16, act_bytes(s->g, 16), c->stream);
         for (auto &p : s->gw)
-            if ((rc = alloc_zero((void **)&p, act_bytes(s->g, s->W), c->stream))) return rc;
+            if (!rc) rc = alloc_zero((void **)&p, act_bytes(s->g, s->W), c->stream);
         for (auto &p : s->zp)
-            if ((rc = alloc_zero((void **)&p, act_bytes(s->g, s->W), c->stream))) return rc;
+            if (!rc) rc = alloc_zero((void **)&p, act_bytes(s->g, s->W), c->stream);
+        if (rc) {
+            cudaDeviceSynchronize();
+            free_train(s);
+            return rc;
+        }
+        s->train_ready = true;
     }
     return PPF_OK;
 }
@@ -661,6 +675,7 @@ extern "C" int ppf_surrogate_predict(ppf_surrogate *s, ppf_ctx *c, double *out3)
     if (rc) return rc;
     const size_t elems = (size_t)c->g.total * 3;
     if (s->scratch_elems != elems) {
+        cudaDeviceSynchronize();
         cudaFree(s->scratch);
         cudaFree(s->stage);
         s->scratch = nullptr;

@@ -27,12 +27,17 @@ def test_512_cubed(precision, steps, drift):
     with ppf.Simulation((N, N, N), ppf.params_default(dt=DT), bc="periodic", precision=precision) as s:
         s.upload(*st)
         r0 = s.reduce()
+        p0 = s.particles(0.5)
         s.step(steps)
         r1 = s.reduce()
-        p = s.particles(0.5)
+        p1 = s.particles(0.5)
     assert r1["nonfinite"] == 0 and r1["steps"] == steps
     assert abs(r1["mass"] / r0["mass"] - 1.0) < drift
     # the pattern's solid blocks: 12 sign regions per axis on the periodic torus
-    # (the end regions join across the boundary), half of the 12^3 products positive
-    assert p["count"] == 864
+    # (the end regions join across the boundary), half of the 12^3 products
+    # positive (the oracle's labeller gives the same on smaller grids)
+    assert p0["count"] == 864
+    # positive blocks touch along their edges, and relaxing the interfaces
+    # joins them: fewer, never more, particles afterwards
+    assert 1 <= p1["count"] <= 864
     assert r1["free_energy"] <= r0["free_energy"]

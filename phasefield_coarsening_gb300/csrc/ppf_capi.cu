@@ -363,8 +363,8 @@ extern "C" int ppf_reduce(ppf_ctx *c, ppf_stats *out) {
     if (!c || !out) return seterr(PPF_EINVAL, "null argument");
     if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
     const int64_t cells = (int64_t)c->nz * c->ny * c->nx;
-    int nb = (int)((cells + 255) / 256);
-    if (nb > 4 * c->num_sms) nb = 4 * c->num_sms;
+    int nb = c->ny * c->nz;                     // one block per x row at most
+    if (nb > 8 * c->num_sms) nb = 8 * c->num_sms;
     int rc = ensure_partials(c, 5 * nb);
     if (rc) return rc;
     if (c->prec == PPF_F32)

@@ -127,40 +127,44 @@ cudaError_t launch_unpack(const Geom &g, Fields<const T> src, double *dst3, cuda
 
 template <typename T>
 __global__ void __launch_bounds__(256) observe_kernel(Geom g, CoefD kd, Fields<const T> f, double *partials) {
-    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
     const T AS = (T)kd.AS, AL = (T)kd.AL, dA = (T)kd.dA, cS0 = (T)kd.cS0, cL0 = (T)kd.cL0;
     const T CS = (T)kd.CS, CL = (T)kd.CL, tmp2 = (T)kd.tmp2, m = (T)kd.m, gam = (T)kd.gamma;
     const T kg = (T)kd.kappa_h2_half;
     double acc[5] = {0, 0, 0, 0, 0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int x = (int)(i % g.nx);
-        const int y = (int)((i / g.nx) % g.ny);
-        const int z = (int)(i / ((int64_t)g.nx * g.ny));
-        const int64_t j = g.at(x, y, z);
-        const T eS = f.eS[j], eL = f.eL[j], c = f.c[j];
-        if (!isfinite((double)eS) || !isfinite((double)eL) || !isfinite((double)c)) {
-            acc[4] += 1.0;
-            continue;
+    // one block per x row (grid-stride over rows): no per-cell index division
+    const int nrows = g.ny * g.nz;
+    for (int rr = blockIdx.x; rr < nrows; rr += gridDim.x) {
+        const int64_t j0 = g.at(0, rr % g.ny, rr / g.ny);
+        for (int x = threadIdx.x; x < g.nx; x += blockDim.x) {
+            const int64_t j = j0 + x;
+            const T eS = f.eS[j], eL = f.eL[j], c = f.c[j];
+            if (!isfinite(eS) || !isfinite(eL) || !isfinite(c)) {
+                acc[4] += 1.0;
+                continue;
+            }
+            // +x/+y/+z neighbours read through the ghost layer (periodic wrap or no-flux copy)
+            const T sx = f.eS[j + 1], sy = f.eS[j + g.P], sz = f.eS[j + g.PS];
+            const T lx = f.eL[j + 1], ly = f.eL[j + g.P], lz = f.eL[j + g.PS];
+            const T s2 = eS * eS + eL * eL;
+            const T h = eS * eS / s2;
+            const T f0 = eS * eS * eS * eS / T(4) - eS * eS / T(2) + eL * eL * eL * eL / T(4) - eL * eL / T(2) +
+                         gam * eS * eS * eL * eL + T(0.25);
+            const T gr = (sx - eS) * (sx - eS) + (lx - eL) * (lx - eL) + (sy - eS) * (sy - eS) +
+                         (ly - eL) * (ly - eL) + (sz - eS) * (sz - eS) + (lz - eL) * (lz - eL);
+            const T rA = T(1) / (AS + dA * h);
+            const T cSp = rA * (AL * c + (T(1) - h) * tmp2);
+            const T cLp = rA * (AS * c - h * tmp2);
+            const T fS = T(0.5) * AS * (cSp - cS0) * (cSp - cS0) + CS;
+            const T fL = T(0.5) * AL * (cLp - cL0) * (cLp - cL0) + CL;
+            acc[0] += (double)c;
+            acc[1] += (double)h;
+            acc[2] += eS > T(0.5) ? 1.0 : 0.0;
+            // the terms differ by orders of magnitude (the parabola offsets CS, CL
+            // against gradient and well terms): summed in double
+            acc[3] += ((double)(m * f0) + (double)(kg * gr)) + ((double)(h * fS) + (double)((T(1) - h) * fL));
         }
-        // +x/+y/+z neighbours read through the ghost layer (periodic wrap or no-flux copy)
-        const T sx = f.eS[j + 1], sy = f.eS[j + g.P], sz = f.eS[j + g.PS];
-        const T lx = f.eL[j + 1], ly = f.eL[j + g.P], lz = f.eL[j + g.PS];
-        const T s2 = eS * eS + eL * eL;
-        const T h = eS * eS / s2;
-        const T f0 = eS * eS * eS * eS / T(4) - eS * eS / T(2) + eL * eL * eL * eL / T(4) - eL * eL / T(2) +
-                     gam * eS * eS * eL * eL + T(0.25);
-        const T gr = (sx - eS) * (sx - eS) + (lx - eL) * (lx - eL) + (sy - eS) * (sy - eS) + (ly - eL) * (ly - eL) +
-                     (sz - eS) * (sz - eS) + (lz - eL) * (lz - eL);
-        const T rA = T(1) / (AS + dA * h);
-        const T cSp = rA * (AL * c + (T(1) - h) * tmp2);
-        const T cLp = rA * (AS * c - h * tmp2);
-        const T fS = T(0.5) * AS * (cSp - cS0) * (cSp - cS0) + CS;
-        const T fL = T(0.5) * AL * (cLp - cL0) * (cLp - cL0) + CL;
-        acc[0] += (double)c;
-        acc[1] += (double)h;
-        acc[2] += eS > T(0.5) ? 1.0 : 0.0;
-        acc[3] += kd.vol * ((double)(m * f0) + (double)(kg * gr) + (double)(h * fS) + (double)((T(1) - h) * fL));
     }
+    acc[3] *= kd.vol;
     block_sum_store<256, 5>(acc, partials, blockIdx.x);
 }
 

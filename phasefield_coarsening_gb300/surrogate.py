@@ -96,12 +96,14 @@ class Stepper:
     """Surrogate + corrector time stepping of one FP32 state."""
 
     def __init__(self, net: Surrogate, sim: Simulation, calls=10, corrector_steps=50, vf_tol=0.005,
-                 f_tol=1e-7, check=True):
+                 f_tol=1e-7, check=True, snapshot=None):
         self.net, self.sim = net, sim
         self.k = int(net.config["k_steps"])
         self.calls, self.corrector_steps, self.vf_tol, self.f_tol, self.check = \
             calls, corrector_steps, vf_tol, f_tol, check
-        self.snap = Simulation(sim.shape, sim.params, "periodic" if sim.bc == 0 else "noflux", "f32") if check else None
+        if check and snapshot is None:
+            snapshot = Simulation(sim.shape, sim.params, "periodic" if sim.bc == 0 else "noflux", "f32")
+        self.snap = snapshot if check else None
         self.mass = sim.reduce()["mass"]       # conserved by the model: every cycle ends on it
         self.cycles = 0
         self.fallbacks = 0

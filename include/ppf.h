@@ -300,6 +300,11 @@ int ppf_surrogate_train_step(ppf_surrogate *s, ppf_ctx *input, ppf_ctx *target, 
 int ppf_surrogate_predict(ppf_surrogate *s, ppf_ctx *ctx, double *out3);
 /* ncalls surrogate calls on ctx's state (k_steps each, mass projected after each). */
 int ppf_surrogate_advance(ppf_surrogate *s, ppf_ctx *ctx, int ncalls);
+/* Test hook (as ppf_debug_inject): with PPF_INJECT_STALL_WAIT the next
+ * convolution launch waits for an input row that never completes, its
+ * bounded wait runs out (ppf_set_wait_limit of the context it runs on) and
+ * the context's next synchronising call returns PPF_ETIMEOUT. */
+int ppf_surrogate_debug_inject(ppf_surrogate *s, int fault);
 
 /* Message for the calling thread's last failure ("" if none). */
 const char *ppf_last_error(void);

@@ -34,7 +34,8 @@ EXPORTS = (
     "ppf_ensemble_autotune", "ppf_mass_project", "ppf_copy_state", "ppf_surrogate_config_default",
     "ppf_surrogate_create", "ppf_surrogate_destroy", "ppf_surrogate_get_config", "ppf_surrogate_num_params",
     "ppf_surrogate_set_params", "ppf_surrogate_get_params", "ppf_surrogate_loss_grad", "ppf_surrogate_train_step",
-    "ppf_surrogate_predict", "ppf_surrogate_advance", "ppf_last_error", "ppf_version",
+    "ppf_surrogate_predict", "ppf_surrogate_advance", "ppf_surrogate_debug_inject", "ppf_last_error",
+    "ppf_version",
     "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_write3d_meta", "ppf_h5_last_error",
 )
 
@@ -162,6 +163,7 @@ def lib() -> ctypes.CDLL:
                                                ctypes.POINTER(ctypes.c_double)]
         L.ppf_surrogate_predict.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.ppf_surrogate_advance.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.ppf_surrogate_debug_inject.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.ppf_h5_dims.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.ppf_h5_read3d.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _dp,
                                     ctypes.c_int64]
@@ -385,6 +387,9 @@ class Surrogate:
 
     def advance(self, sim: Simulation, ncalls: int = 1):
         _check(lib().ppf_surrogate_advance(self._h, sim._h, int(ncalls)))
+
+    def debug_inject(self, fault: int = INJECT_STALL_WAIT):
+        _check(lib().ppf_surrogate_debug_inject(self._h, int(fault)))
 
 
 class Ensemble:

@@ -74,6 +74,7 @@ struct ConvArgs {
     int items;
     int *err;
     unsigned long long limit_ns;
+    int inject_stall;       // test hook: one input row's copies never complete
 };
 
 struct WgradArgs {

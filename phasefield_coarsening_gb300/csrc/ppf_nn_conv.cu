@@ -255,7 +255,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv_kernel(const ConvArgs a)
                         ok = false;
                         break;
                     }
-                    mbar_expect_tx(full(s), C::ROWB);
+                    // test hook: the second row's barrier expects 16 bytes that never come
+                    mbar_expect_tx(full(s), C::ROWB + ((a.inject_stall && q == 1) ? 16u : 0u));
 #pragma unroll
                     for (int k = 0; k < C::RING; ++k)
                         if (k == (int)s) issued_q[k] = q;

@@ -255,6 +255,7 @@ struct ppf_surrogate {
     double *stage = nullptr;
     size_t scratch_elems = 0;
     int conv_grid[2][2] = {}, wgrad_grid = 0;
+    int inject = 0;              // test hook: the next convolution's wait runs out
 };
 
 namespace {
@@ -364,7 +365,10 @@ ConvArgs conv_args(ppf_surrogate *s, ppf_ctx *c, int layer, const uint16_t *x, c
 
 int run_conv(ppf_surrogate *s, ppf_ctx *c, int ci, int co, int epi, const ConvArgs &a) {
     const int grid = s->conv_grid[ci == 32][co == 32];
-    SCU(launch_conv(ci, co, epi, a, grid, c->stream));
+    ConvArgs b = a;
+    b.inject_stall = s->inject;
+    s->inject = 0;
+    SCU(launch_conv(ci, co, epi, b, grid, c->stream));
     return PPF_OK;
 }
 
@@ -719,6 +723,13 @@ extern "C" int ppf_surrogate_advance(ppf_surrogate *s, ppf_ctx *c, int ncalls) {
         c->steps += s->cfg.k_steps;
         if ((rc = project(c, true))) return rc;
     }
+    return PPF_OK;
+}
+
+extern "C" int ppf_surrogate_debug_inject(ppf_surrogate *s, int fault) {
+    if (!s) return serr(PPF_EINVAL, "null surrogate");
+    if (fault != PPF_INJECT_NONE && fault != PPF_INJECT_STALL_WAIT) return serr(PPF_EINVAL, "unknown fault");
+    s->inject = fault == PPF_INJECT_STALL_WAIT;
     return PPF_OK;
 }
 

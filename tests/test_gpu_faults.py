@@ -39,3 +39,33 @@ def test_wait_limit_validation():
             s.set_wait_limit(0.0)
         with pytest.raises(ppf.PPFError):
             s.debug_inject(99)
+
+
+def test_surrogate_wait_limit_expiry_is_reported_and_recovers():
+    """The same for the tensor-core convolution: one input row's copies never
+    complete, the bounded waits run out, every role drains and exits, the
+    host sees PPF_ETIMEOUT, and the next call is exact again."""
+    from oracle import surrogate_ref as sr
+    shape = (6, 5, 128)
+    st = smooth_state(shape, seed=9)
+    p = sr.init_params(16, seed=2, last_scale=0.3)
+    with ppf.Surrogate(width=16) as net, ppf.Simulation(shape, bc="periodic", precision="f32") as s:
+        net.set_params(p)
+        s.upload(*st)
+        s.set_wait_limit(0.05)
+        net.debug_inject(ppf.INJECT_STALL_WAIT)
+        net.advance(s, 1)
+        with pytest.raises(ppf.PPFError) as e:
+            s.sync()
+        assert e.value.code == -6
+        s.set_wait_limit(1.0)
+        s.upload(*st)
+        net.advance(s, 1)
+        got = s.download()
+    with ppf.Surrogate(width=16) as net2, ppf.Simulation(shape, bc="periodic", precision="f32") as s2:
+        net2.set_params(p)
+        s2.upload(*st)
+        net2.advance(s2, 1)
+        ref = s2.download()
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)

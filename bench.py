@@ -199,7 +199,7 @@ def surrogate_section(state, shape):
             continue
         net = S.load(path)
         cfg = net.config
-        res = S.judge(net, state, cycles=12, calls=10, corrector_steps=50, warmup=500)
+        res = S.compare_to_stencil(net, state, cycles=12, calls=10, corrector_steps=50, warmup=500)
         res.pop("trajectory")
         sim = ppf.Simulation(shape, ppf.params_default(dt=DT), "periodic", "f32")
         sim.upload(*state)

@@ -205,7 +205,7 @@ int ppf_autotune(ppf_ctx *ctx, int trial_steps, ppf_tune *best);
  * host application calls between its own steps, whose device memory belongs
  * to the application's pool or arena (a caching allocator, preallocated
  * communication buffers), where an unplanned cudaMalloc can fail on a full
- * device, fragment the pool, or hold up the application's streams.  The
+ * device, fragment its memory pool, or hold up the application's streams.  The
  * caller passes its own device arrays -- etaS, etaL, c, each nz*ny*nx
  * doubles in C order [z][y][x] -- and a device array `out` of 5 doubles; the
  * call queues the reduction on `stream` (NULL: the default stream) and

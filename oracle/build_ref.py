@@ -1,6 +1,6 @@
 """ORACLE -- test infrastructure.  Recipe that compiles the reference program
 itself (jijn/phasefield_coarsening phasefield.c) as a second, independent
-checker and as the CPU baseline.
+oracle and as the CPU baseline.
 
 The reference fixes its configuration at compile time with unguarded
 #defines and const locals, and it needs MPI and libhdf5, neither of which is

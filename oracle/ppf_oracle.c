@@ -2,7 +2,7 @@
  * ORACLE -- test infrastructure, not product code.
  *
  * A plain-C restatement of the reference's explicit step, used only as the
- * checker by tests/, by __graft_entry__.smoke() and by bench.py's CPU
+ * oracle by tests/, by __graft_entry__.smoke() and by bench.py's CPU
  * baseline leg.  Nothing in the product links or calls it.
  *
  * It follows jijn/phasefield_coarsening phasefield.c line by line:

@@ -6,7 +6,7 @@
 // steps, whose device memory is owned by the application's pool or arena
 // (a caching allocator, a preallocated MPI/NCCL buffer set), where a
 // cudaMalloc the owner did not plan for can fail on a full device, fragment
-// the pool, or stall the application's streams while the driver maps new
+// the application's memory pool, or stall the application's streams while the CUDA driver maps new
 // memory.  Such a caller holds the fields in its own device buffers and only
 // wants five numbers back.
 //

@@ -3,7 +3,7 @@
 // one call), its training on the device, and the FP64 solute-mass
 // projection.  No counterpart in the reference: the reference only has
 // the explicit step (phasefield.c:301-476) that this network stands in for
-// and that trains, corrects and judges it.
+// and that trains it, corrects it and measures its error.
 //
 // Network: six 3x3x3 convolutions, 16 -> W -> W -> W -> W -> W -> 16
 // channels (W = 16 or 32), SiLU after the first five, residual output:

@@ -14,7 +14,7 @@ in one call.  This module holds what surrounds it:
   solute mass projected in FP64 after every call; a cycle whose result
   fails the checks (non-finite cells, free energy rising, solid fraction
   drifting) is redone with the stencil alone (the fallback);
-* judge -- the surrogate arm against the plain stencil from the same
+* compare_to_stencil -- the surrogate arm against the plain stencil from the same
   state: mean particle radius, solid fraction, free energy, solute mass.
 """
 from __future__ import annotations
@@ -137,7 +137,7 @@ class Stepper:
         return self.steps_per_cycle
 
 
-def judge(net: Surrogate, state, cycles=10, calls=10, corrector_steps=50, warmup=0, threshold=0.5,
+def compare_to_stencil(net: Surrogate, state, cycles=10, calls=10, corrector_steps=50, warmup=0, threshold=0.5,
           params=None, check=True):
     """Advance `state` with the surrogate + corrector and with the plain FP32
     stencil for the same simulated time; after every cycle compare mean

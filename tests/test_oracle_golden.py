@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
+import oracle.build_ref as build_ref
 from helpers import golden_cases, golden_dt, load_golden, smooth_state
 
 # bit-exact on x86-64 gcc -O2 (no FMA contraction); arm64 gcc contracts
@@ -53,10 +54,10 @@ def test_oracle_conserves_solute_periodic_and_noflux():
         assert abs(c.sum() - m0) <= 1e-12 * abs(m0)
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/phasefield.c"), reason="reference sources absent")
+@pytest.mark.skipif(not os.path.exists(build_ref.REF_SRC), reason="reference sources absent")
 @pytest.mark.parametrize("bc", [0, 1])
 def test_oracle_matches_fresh_reference_build(bc, tmp_path):
-    import oracle.build_ref as br
+    br = build_ref
     from phasefield_coarsening_gb300 import read_fields, write_fields
     shape = (7, 9, 11)
     st = smooth_state(shape, seed=11 + bc)

@@ -217,7 +217,8 @@ def surrogate_section(state, shape):
         out.append({
             "weights": name, "width": w, "k_steps": cfg["k_steps"], "calls_per_cycle": 10, "corrector_steps": 50,
             "sim_time_per_wall_s": res["sim_time_per_wall_s"], "speedup_vs_stencil": round(res["speedup"], 3),
-            "max_rel_err": res["max_rel_err"], "mass_drift": res["mass_drift"], "steps": res["steps"],
+            "max_rel_err": res["max_rel_err"], "field_err_vs_change": res["field_err_vs_change"],
+            "mass_drift": res["mass_drift"], "steps": res["steps"],
             "fallbacks": res["fallbacks"], "ms_per_call": round(call_s * 1e3, 3),
             "roofline": {"bound": "tensor", "achieved": round(tf, 1), "peak": peak, "unit": "TFLOP/s",
                          "frac": round(tf / peak, 4) if peak else None,

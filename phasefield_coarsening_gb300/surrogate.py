@@ -142,8 +142,11 @@ def compare_to_stencil(net: Surrogate, state, cycles=10, calls=10, corrector_ste
     """Advance `state` with the surrogate + corrector and with the plain FP32
     stencil for the same simulated time; after every cycle compare mean
     particle radius, solid fraction and free energy.  Returns a dict of the
-    largest relative errors, the surrogate arm's solute-mass drift and both
-    arms' simulated time per wall second (device-synchronised timing)."""
+    largest relative errors, the surrogate arm's solute-mass drift, both
+    arms' simulated time per wall second (device-synchronised timing), and
+    field-space errors at the end: per field ||sur - ref|| / ||ref - start||,
+    for the surrogate arm and for the same schedule without the network
+    (the calls replaced by the identity, the corrector steps kept)."""
     shape = state[0].shape
     prm = params if params is not None else params_default(dt=DT)
     ref = Simulation(shape, prm, "periodic", "f32")
@@ -153,6 +156,7 @@ def compare_to_stencil(net: Surrogate, state, cycles=10, calls=10, corrector_ste
         ref.step(warmup)
     sur.copy_from(ref)
     m0 = sur.reduce()["mass"]
+    x0 = sur.download()
     stepper = Stepper(net, sur, calls=calls, corrector_steps=corrector_steps, check=check)
     err = {"rbar": 0.0, "solid": 0.0, "free_energy": 0.0}
     t_sur = t_ref = 0.0
@@ -179,8 +183,22 @@ def compare_to_stencil(net: Surrogate, state, cycles=10, calls=10, corrector_ste
         rows.append({"steps": steps, "rbar_sur": ps["mean_radius"], "rbar_ref": pr["mean_radius"],
                      "count_sur": ps["count"], "count_ref": pr["count"], **{"err_" + kk: v for kk, v in e.items()}})
     m1 = sur.reduce()["mass"]
+    # field space: what the network captured of the stencil's change
+    xs, xr = sur.download(), ref.download()
+    ident = Simulation(shape, prm, "periodic", "f32")
+    ident.upload(*x0)
+    ident.step(cycles * corrector_steps)
+    xi = ident.download()
+    ident.close()
+    names = ("etaS", "etaL", "c")
+
+    def rel(a, b, base):
+        return {n: float(np.linalg.norm(p - q) / max(np.linalg.norm(q - o), 1e-300))
+                for n, p, q, o in zip(names, a, b, base)}
+    field = {"surrogate": rel(xs, xr, x0), "identity": rel(xi, xr, x0)}
     dt = prm.dt
-    out = {"max_rel_err": err, "mass_drift": abs(m1 / m0 - 1.0), "steps": steps, "cycles": cycles,
+    out = {"max_rel_err": err, "field_err_vs_change": field, "mass_drift": abs(m1 / m0 - 1.0), "steps": steps,
+           "cycles": cycles,
            "fallbacks": stepper.fallbacks, "sim_time_per_wall_s": {"surrogate": steps * dt / t_sur,
                                                                     "stencil": steps * dt / t_ref},
            "speedup": t_ref / t_sur, "trajectory": rows}

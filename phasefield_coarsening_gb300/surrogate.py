@@ -226,13 +226,14 @@ def load(path: str) -> Surrogate:
     return net
 
 
-def fit(width=16, k=50, iters=2000, shape=(64, 128, 128), seed=1, lr=1e-3, lr_final=1e-4, log_every=250):
+def fit(width=16, k=50, iters=2000, shape=(64, 128, 128), seed=1, lr=1e-3, lr_final=1e-4, log_every=250,
+        loss_weight=(1.0, 1.0, 1.0)):
     """Train a fresh network on stencil trajectories (output scales from
     the data, zero-initialised output layer); returns (net, log)."""
     stream = PairStream(shape=shape, k=k, seed=seed)
     try:
         scales = calibrate(stream, n=3)
-        net = Surrogate(width=width, k_steps=k, out_scale=scales)
+        net = Surrogate(width=width, k_steps=k, out_scale=scales, loss_weight=list(loss_weight))
         net.set_params(init_params(width, seed=seed))
         log = train(net, stream, iters, lr=lr, lr_final=lr_final, log_every=log_every)
     finally:
@@ -266,6 +267,7 @@ if __name__ == "__main__":
     ap.add_argument("--k", type=int, default=50)
     ap.add_argument("--iters", type=int, default=2000)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--loss-weight", type=float, nargs=3, default=(1.0, 1.0, 1.0), metavar=("ETAS", "ETAL", "C"))
     ap.add_argument("--out")
     ap.add_argument("--profile-call", type=int, metavar="EDGE",
                     help="instead of training: one surrogate call on an EDGE^3 FP32 state (a fixed launch "
@@ -288,6 +290,7 @@ if __name__ == "__main__":
     if not a.out:
         ap.error("--out is required for training")
     t0 = time.time()
-    net, log = fit(width=a.width, k=a.k, iters=a.iters, seed=a.seed)
-    save(net, a.out, iters=a.iters, seed=a.seed, train_s=round(time.time() - t0, 1), log=log)
+    net, log = fit(width=a.width, k=a.k, iters=a.iters, seed=a.seed, loss_weight=a.loss_weight)
+    save(net, a.out, iters=a.iters, seed=a.seed, loss_weight=list(a.loss_weight),
+         train_s=round(time.time() - t0, 1), log=log)
     print(json.dumps({"out": a.out, "train_s": round(time.time() - t0, 1), "log": log}))

@@ -227,10 +227,10 @@ def load(path: str) -> Surrogate:
 
 
 def fit(width=16, k=50, iters=2000, shape=(64, 128, 128), seed=1, lr=1e-3, lr_final=1e-4, log_every=250,
-        loss_weight=(1.0, 1.0, 1.0)):
+        loss_weight=(1.0, 1.0, 1.0), warmup=200, segment=25):
     """Train a fresh network on stencil trajectories (output scales from
     the data, zero-initialised output layer); returns (net, log)."""
-    stream = PairStream(shape=shape, k=k, seed=seed)
+    stream = PairStream(shape=shape, k=k, seed=seed, warmup=warmup, segment=segment)
     try:
         scales = calibrate(stream, n=3)
         net = Surrogate(width=width, k_steps=k, out_scale=scales, loss_weight=list(loss_weight))
@@ -268,6 +268,8 @@ if __name__ == "__main__":
     ap.add_argument("--iters", type=int, default=2000)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--loss-weight", type=float, nargs=3, default=(1.0, 1.0, 1.0), metavar=("ETAS", "ETAL", "C"))
+    ap.add_argument("--warmup", type=int, default=200, help="stencil steps before a new trajectory's first pair")
+    ap.add_argument("--segment", type=int, default=25, help="pairs per trajectory")
     ap.add_argument("--out")
     ap.add_argument("--profile-call", type=int, metavar="EDGE",
                     help="instead of training: one surrogate call on an EDGE^3 FP32 state (a fixed launch "
@@ -290,7 +292,8 @@ if __name__ == "__main__":
     if not a.out:
         ap.error("--out is required for training")
     t0 = time.time()
-    net, log = fit(width=a.width, k=a.k, iters=a.iters, seed=a.seed, loss_weight=a.loss_weight)
-    save(net, a.out, iters=a.iters, seed=a.seed, loss_weight=list(a.loss_weight),
-         train_s=round(time.time() - t0, 1), log=log)
+    net, log = fit(width=a.width, k=a.k, iters=a.iters, seed=a.seed, loss_weight=a.loss_weight, warmup=a.warmup,
+                   segment=a.segment)
+    save(net, a.out, iters=a.iters, seed=a.seed, loss_weight=list(a.loss_weight), warmup=a.warmup,
+         segment=a.segment, train_s=round(time.time() - t0, 1), log=log)
     print(json.dumps({"out": a.out, "train_s": round(time.time() - t0, 1), "log": log}))

@@ -24,6 +24,7 @@ from __future__ import annotations
 import numpy as np
 
 LAYERS = 6
+N_FEATURES = 5          # input channels in use (etaS, etaL, composition, two BF16 residuals)
 
 
 def bf16(a):
@@ -64,7 +65,7 @@ def init_params(width, seed=0, last_scale=0.0):
     rng = np.random.default_rng(seed)
     layers = []
     for li, (ci, co) in enumerate(layer_channels(width)):
-        ci_used = 3 if li == 0 else ci
+        ci_used = N_FEATURES if li == 0 else ci
         co_used = 3 if li == LAYERS - 1 else co
         a = np.sqrt(3.0 / (27 * ci_used))
         W = np.zeros((27, co, ci))
@@ -137,8 +138,10 @@ def features(eS, eL, c, cfg):
     h = s2 / np.maximum(s2 + l2, np.float32(1e-30))
     cS, cL, kc = np.float32(cfg["c_solid"]), np.float32(cfg["c_liquid"]), np.float32(cfg["in_scale_c"])
     f2 = (c - (cL + (cS - cL) * h)) * kc
+    rS = (eS - bf16(eS).astype(np.float32)) * np.float32(256.0)
+    rL = (eL - bf16(eL).astype(np.float32)) * np.float32(256.0)
     f = np.zeros((16,) + eS.shape)
-    f[0], f[1], f[2] = eS, eL, f2
+    f[0], f[1], f[2], f[3], f[4] = eS, eL, f2, rS, rL
     return f
 
 

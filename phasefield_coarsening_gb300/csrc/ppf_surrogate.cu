@@ -9,12 +9,13 @@
 // channels (W = 16 or 32), SiLU after the first five, residual output:
 //   state(t + k dt) = state(t) + out_scale * net(features(state(t)))
 // for the three fields (etaS, etaL, c); output channels 3..15 and input
-// channels 3..15 are zero padding that keeps every GEMM K and N a multiple
-// of 16.  Input features: etaS, etaL and (c - c_eq(h)) * in_scale_c with
+// channels 5..15 are zero padding that keeps every GEMM K and N a multiple
+// of 16.  Input features: etaS, etaL, (c - c_eq(h)) * in_scale_c with
 // h = etaS^2 / (etaS^2 + etaL^2) (the reference's interpolation,
 // phasefield.c:331) and c_eq(h) = h c_solid + (1-h) c_liquid, so the
 // composition enters as its (small) departure from local equilibrium,
-// which BF16 represents to 2^-8 relative.
+// which BF16 represents to 2^-8 relative; then 256 (etaS - bf16(etaS)) and
+// 256 (etaL - bf16(etaL)), the part of each phase field BF16 drops.
 //
 // After every call the solute mass sum(c) is projected back, in FP64, to
 // its value before the call: the deficit is spread over the cells as whole
@@ -110,7 +111,12 @@ __global__ void __launch_bounds__(kNT) features_kernel(Geom sg, Fields<const flo
             const float s2 = eS * eS, l2 = eL * eL;
             const float h = s2 / fmaxf(s2 + l2, 1e-30f);
             const float f2 = (c - (cL + (cS - cL) * h)) * kc;
-            const uint4 v = make_uint4(pack2(eS, eL), pack2(f2, 0.f), 0u, 0u);
+            // what BF16 drops of etaS and etaL, scaled into range: with
+            // channels 0-1 the network sees both fields to ~16 bits
+            const uint32_t hi = pack2(eS, eL);
+            const float rS = (eS - __uint_as_float(hi << 16)) * 256.0f;
+            const float rL = (eL - __uint_as_float(hi & 0xFFFF0000u)) * 256.0f;
+            const uint4 v = make_uint4(hi, pack2(f2, rS), pack2(rL, 0.f), 0u);
             const int ax = image_of(x, g.nx, g.bc);
             for (int k = 0; k < 8; ++k) {
                 const int xx = (k & 1) ? ax : x, yy = (k & 2) ? ay : y, zz = (k & 4) ? az : z;

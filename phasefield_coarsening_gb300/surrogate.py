@@ -250,7 +250,7 @@ def init_params(width, seed=0):
     parts = []
     for li in range(6):
         ci, co = chans[li], chans[li + 1]
-        ci_used = 3 if li == 0 else ci
+        ci_used = 5 if li == 0 else ci         # etaS, etaL, composition, two BF16 residuals
         W = np.zeros((27, co, ci))
         if li < 5:
             a = math.sqrt(3.0 / (27 * ci_used))

@@ -47,7 +47,7 @@ def test_backward_matches_finite_differences():
     for li, (ci, co) in enumerate(sr.layer_channels(16)):
         n = 27 * co * ci
         W = np.arange(off, off + n).reshape(27, co, ci)
-        used_ci = 3 if li == 0 else ci
+        used_ci = sr.N_FEATURES if li == 0 else ci
         used_co = 3 if li == sr.LAYERS - 1 else co
         idx += list(rng.choice(W[:, :used_co, :used_ci].ravel(), 4, replace=False))
         off += n
@@ -68,6 +68,19 @@ def test_flatten_roundtrip_and_zero_padding():
     layers = sr.unflatten(p, 32)
     assert np.array_equal(sr.flatten(layers).astype(np.float32), p)
     W0, _ = layers[0]
-    assert not W0[:, :, 3:].any()          # padded input channels
+    assert not W0[:, :, sr.N_FEATURES:].any()          # padded input channels
     W5, b5 = layers[-1]
     assert not W5[:, 3:, :].any() and not b5.any()
+
+
+def test_features_carry_what_bf16_drops():
+    rng = np.random.default_rng(3)
+    eS = rng.random((2, 3, 4)).astype(np.float32)
+    eL = (1 - eS).astype(np.float32)
+    c = np.full(eS.shape, 0.9, np.float32)
+    f = sr.features(eS, eL, c, CFG)
+    # hi + lo reconstructs the FP32 field to far better than BF16 alone
+    for k, x in ((3, eS), (4, eL)):
+        rec = sr.bf16(x) + sr.bf16(f[k]) / 256.0
+        assert np.abs(rec - x).max() < 2.0 ** -16 * 1.01
+        assert np.abs(sr.bf16(x) - x).max() > 2.0 ** -14

@@ -438,35 +438,54 @@ def run_ensemble(args):
 
 
 def run_reference(args):
+    """The reference's own CPU implementation of the step on the host cores:
+    the reference program (phasefield.c, patched serial build with OpenMP on
+    its three passes, oracle/build_ref.py) when it can be built here, else
+    the oracle restatement (C, OpenMP).  Rank 0 only."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import numpy as np
 
+    import oracle
     import oracle.build_ref as br
     import __graft_entry__ as ge
     from phasefield_coarsening_gb300 import ic, write_fields
     ncores = os.cpu_count() or 1
-    try:
-        exe = br.build(**ge.REF_BENCH)
-    except Exception as e:
-        print(json.dumps({"impl": "reference", "unavailable": f"reference build failed: {str(e)[:200]}"}))
-        return
     eS, eL, c, info = ic.workload(WORKLOAD, seed=args.seed)
     cells = int(np.prod(eS.shape))
     steps_per_run = ge.REF_BENCH["n_iter"]
-    with tempfile.TemporaryDirectory() as td:
-        inp = os.path.join(td, "in.h5")
-        write_fields(inp, eS, eL, c)
+    try:
+        exe = br.build(**ge.REF_BENCH)
+        kind = "reference"
+    except Exception as e:               # no reference sources nor patched unit: the oracle port
+        print(f"reference program unavailable ({str(e)[:120]}); timing the oracle restatement", file=sys.stderr)
+        exe, kind = None, "port"
+    loop = []
+    if exe is not None:
+        with tempfile.TemporaryDirectory() as td:
+            inp = os.path.join(td, "in.h5")
+            write_fields(inp, eS, eL, c)
+            for _ in range(args.warmup):
+                br.run(exe, inp, threads=ncores, timeout=1800)
+            for _ in range(args.steps):
+                r = br.run(exe, inp, threads=ncores, timeout=1800)
+                if r["rc"] != 0 or not r["loop_s"]:
+                    print(json.dumps({"impl": "reference", "unavailable": "reference run failed: " + r["stderr"][-200:]}))
+                    return
+                loop.append(r["loop_s"])
+        sample = (f"{steps_per_run} time steps per run of the reference phasefield.c (serial build + OpenMP on "
+                  f"sweep_fields, gcc -O2), {ncores} threads")
+    else:
+        prm = oracle.reference_params(dt=DT)
         for _ in range(args.warmup):
-            br.run(exe, inp, threads=ncores, timeout=1800)
-        loop = []
+            oracle.run(eS, eL, c, steps_per_run, bc=0, params=prm)
         for _ in range(args.steps):
-            r = br.run(exe, inp, threads=ncores, timeout=1800)
-            if r["rc"] != 0 or not r["loop_s"]:
-                print(json.dumps({"impl": "reference", "unavailable": "reference run failed: " + r["stderr"][-200:]}))
-                return
-            loop.append(r["loop_s"])
+            t0 = time.perf_counter()
+            oracle.run(eS, eL, c, steps_per_run, bc=0, params=prm)
+            loop.append(time.perf_counter() - t0)
+        sample = (f"{steps_per_run} time steps per run of the oracle restatement of phasefield.c's step (C, "
+                  f"OpenMP), {ncores} threads")
     total = sum(loop)
     value = cells * steps_per_run * args.steps / total / 1e9
     line = {
@@ -477,9 +496,8 @@ def run_reference(args):
         "config": {"workload": WORKLOAD, "grid": list(eS.shape), "bc": "periodic", "dt": DT,
                    "time_steps_per_bench_step": steps_per_run, "parallelism": f"OpenMP x{ncores} (host)"},
         "sim_time_per_wall_s": round(value * 1e9 / cells * DT, 1),
-        "cpu_baseline": {"value": round(value, 4), "unit": "GLUPS", "cores": ncores, "kind": "reference",
-                         "sample": f"{steps_per_run} time steps per run of the reference phasefield.c "
-                                   f"(serial build + OpenMP on sweep_fields, gcc -O2), {ncores} threads"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "GLUPS", "cores": ncores, "kind": kind,
+                         "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }

@@ -60,3 +60,27 @@ def test_reference_arm_nonzero_rank_exits_without_work(monkeypatch, capsys):
         steps, warmup, seed = 1, 0, 0
     assert bench.run_reference(A()) is None
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_falls_back_to_the_oracle_port(monkeypatch, capsys):
+    """Without the reference's sources or a patched unit, --impl reference
+    times the oracle restatement and says so (kind "port")."""
+    import json
+
+    import oracle.build_ref as br
+    from phasefield_coarsening_gb300 import ic
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+
+    def no_build(**kw):
+        raise FileNotFoundError("reference sources absent")
+    monkeypatch.setattr(br, "build", no_build)
+    small = ic.workload("spheres64_uniform4to8", seed=0)
+    monkeypatch.setattr(ic, "workload", lambda name, seed=0, shape=None: small)
+
+    class A:
+        steps, warmup, seed = 2, 1, 0
+    bench.run_reference(A())
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["cpu_baseline"]["kind"] == "port"
+    assert line["value"] > 0 and line["unit"] == "GLUPS" and line["e2e"]["h2d_bytes_per_step"] == 0

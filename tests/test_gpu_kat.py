@@ -18,7 +18,8 @@ def slab(shape):
     cS, cL = ic.equilibrium_compositions()
     x = np.arange(shape[2])
     n = shape[2]
-    e1 = 0.5 * (1 + np.tanh(2 * (x - n / 4) / 4.0)) * 0.5 * (1 - np.tanh(2 * (x - 3 * n / 4) / 4.0))
+    # interfaces between grid points (a cell exactly at 0.5 would hide the crossing)
+    e1 = 0.5 * (1 + np.tanh(2 * (x - n / 4 - 0.3) / 4.0)) * 0.5 * (1 - np.tanh(2 * (x - 3 * n / 4 - 0.3) / 4.0))
     eS = np.broadcast_to(e1, shape).copy()
     eL = 1 - eS
     h = eS ** 2 / (eS ** 2 + eL ** 2)

@@ -35,6 +35,10 @@
  *                          /etaL read goes through the closed /etaS
  *                          identifier (:1032) and leaves etaL = 1.0
  *   --timing               print step throughput on stderr at the end
+ *   --mass-project         FP32 runs: put sum(c) back on its initial value
+ *                          (FP64 arithmetic, ppf_mass_project) before every
+ *                          save, so the solute mass does not drift with the
+ *                          FP32 rounding of the per-cell update
  *   --restart              continue the run a saved file belongs to: every
  *                          file written holds a dataset /ppf_restart =
  *                          (next iteration, dt, save number, error); with
@@ -86,7 +90,7 @@ int main(int argc, char **argv)
         return -1;
     }
     const char *input = argv[1];
-    int bc = PPF_BC_NOFLUX, prec = PPF_F64, etaL_bug = 0, timing = 0, restart = 0, dt_given = 0;
+    int bc = PPF_BC_NOFLUX, prec = PPF_F64, etaL_bug = 0, timing = 0, restart = 0, dt_given = 0, mproj = 0;
     int64_t n_iter = 5000001L, n_save = 50000L, n_iter_init = 100000000L;
     double threshold = 1.0e-12, dt = 0.0;
     int64_t chunk[3] = {0, 0, 0};
@@ -113,6 +117,7 @@ int main(int argc, char **argv)
         } else if (!strcmp(o, "--ref-etaL-bug")) etaL_bug = 1;
         else if (!strcmp(o, "--timing")) timing = 1;
         else if (!strcmp(o, "--restart")) restart = 1;
+        else if (!strcmp(o, "--mass-project")) mproj = 1;
         else {
             fprintf(STD_BUF, "Usage:\nppf filename\n");
             return -1;
@@ -173,6 +178,13 @@ int main(int argc, char **argv)
     if (ppf_create((int)dims[0], (int)dims[1], (int)dims[2], &prm, bc, prec, &ctx) != 0)
         return die("device", ppf_last_error());
     if (ppf_upload(ctx, etaS, etaL, c) != 0) return die("upload", ppf_last_error());
+    if (mproj && prec != PPF_F32) return die("--mass-project", "applies to --precision f32");
+    double mass0 = 0.0;
+    if (mproj) {
+        ppf_stats st0;
+        if (ppf_reduce(ctx, &st0) != 0) return die("reduce", ppf_last_error());
+        mass0 = st0.mass;
+    }
 
     /* main loop, :178-258 */
     int64_t i_iter = i_start;
@@ -197,6 +209,7 @@ int main(int argc, char **argv)
         save_iter++;
         ppf_stats st;
         if (ppf_reduce(ctx, &st) != 0) return die("reduce", ppf_last_error());
+        if (mproj && ppf_mass_project(ctx, mass0) != 0) return die("mass projection", ppf_last_error());
         fprintf(STD_BUF, "%ld: c=%10.4e; S=%10.4e; L=%10.4e\t", (long)j, st.sum_dc2, st.sum_detaS2, st.sum_detaL2);
         error = sqrt(st.sum_dc2);
         fprintf(STD_BUF, "iter: %ld; err: %10.4e\n", (long)j, error);

@@ -307,3 +307,24 @@ def test_ppf_restart_continues_the_run_exactly(precision, tmp_path):
         assert np.array_equal(ppf.h5_read(a, "ppf_restart"), ppf.h5_read(b, "ppf_restart"))
     conv = lambda t: [ln for ln in t.splitlines() if ": c=" in ln or ln.startswith("Total steps")]
     assert conv(r.stderr)[1:] == conv(r2.stderr)
+
+
+def test_ppf_mass_project_option_keeps_the_solute_mass(tmp_path):
+    """--mass-project (FP32 runs): every saved state holds the initial sum(c)
+    to FP64 round-off, and the fields differ from a plain run by the few
+    ulps the projection moves."""
+    shape = (16, 20, 24)
+    st = smooth_state(shape, seed=41)
+    inp = str(tmp_path / "m.h5")
+    ppf.write_fields(inp, *st)
+    m0 = float(np.asarray(st[2], np.float32).astype(np.float64).sum())
+    opts = ["--bc", "periodic", "--steps", "2001", "--save", "1000", "--dt", repr(DT08), "--precision", "f32"]
+    r = subprocess.run([ppf.EXE_PATH, inp] + opts + ["--mass-project"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    outs = [ln for ln in r.stdout.splitlines() if ln]
+    assert len(outs) == 2
+    for fn in outs:
+        c = ppf.read_fields(fn)[2]
+        assert abs(c.sum() / m0 - 1.0) < 1e-13
+    r2 = subprocess.run([ppf.EXE_PATH, inp, "--precision", "f64", "--mass-project"], capture_output=True, text=True)
+    assert r2.returncode != 0 and "f32" in r2.stderr

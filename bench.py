@@ -250,7 +250,12 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     sim.set_stream(stream.cuda_stream)
     sim.upload(eS, eL, c)
-    tune = sim.autotune(trial_steps=10)        # the project's launch autotuner (state is kept)
+    if args.launch:
+        # a fixed launch choice (z chunk, unroll), e.g. for a reproducible profile
+        sim.set_tune(args.launch[0], args.launch[1])
+        tune = sim.get_tune()
+    else:
+        tune = sim.autotune(trial_steps=10)    # the project's launch autotuner (state is kept)
 
     def bench_step():
         sim.step(INNER)
@@ -513,6 +518,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--launch", type=int, nargs=2, metavar=("ZC", "ROLL"),
+                    help="fixed launch choice of the stencil (z chunk, unroll 1 or 3) instead of autotuning")
     ap.add_argument("--workload", choices=[WORKLOAD, "ensemble64"], default=WORKLOAD)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

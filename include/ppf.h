@@ -185,7 +185,7 @@ int ppf_particles(ppf_ctx *ctx, double threshold, ppf_particle_stats *out, int64
  * phasefield.c:58-62, :340-350). */
 typedef struct ppf_tune {
     int zc;              /* z planes per work item of the persistent grid */
-    int roll;            /* 3: plane body unrolled three times, 1: one copy */
+    int roll;            /* 1: one plane body (the default), 3: unrolled three times */
     int grid;            /* CTAs (derived from zc; ignored by ppf_set_tune) */
     double us_per_step;  /* measured time of the winner (ppf_autotune only) */
 } ppf_tune;

@@ -277,7 +277,7 @@ class Simulation:
         _check(lib().ppf_get_tune(self._h, ctypes.byref(t)))
         return t.as_dict()
 
-    def set_tune(self, zc: int, roll: int = 3):
+    def set_tune(self, zc: int, roll: int = 1):
         t = Tune(int(zc), int(roll), 0, 0.0)
         _check(lib().ppf_set_tune(self._h, ctypes.byref(t)))
 

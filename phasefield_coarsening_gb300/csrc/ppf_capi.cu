@@ -190,7 +190,7 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
                 return seterr(PPF_ECUDA, "TMA descriptor setup failed (%d)", mr);
             }
         }
-    c->tune.roll = 3;
+    c->tune.roll = 1;
     c->tune.grid = precision == PPF_F32 ? tma_grid<float>(c->g, c->num_sms, &c->tune.zc)
                                         : tma_grid<double>(c->g, c->num_sms, &c->tune.zc);
     if (c->tune.grid < 1) {

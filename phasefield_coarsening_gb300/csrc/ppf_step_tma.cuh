@@ -1,5 +1,6 @@
-// ppf_step_tma.cu -- the fused explicit step as a TMA-fed, z-marching,
-// persistent sm_103a kernel.
+// ppf_step_tma.cuh -- the fused explicit step as a TMA-fed, z-marching,
+// persistent sm_103a kernel (instantiated per precision by ppf_step_f32.cu
+// and ppf_step_f64.cu, which compile in parallel).
 //
 // Replaces, per time step, the reference's BC fill (phasefield.c:1112-1189)
 // and the three passes of sweep_fields (:325-335 pass A, :347-391 pass B,
@@ -21,6 +22,8 @@
 // Every mbarrier wait is bounded by a time limit: on expiry the CTA sets an
 // error word, drains its own outstanding copies (again bounded) and exits
 // uniformly; the host reports PPF_ETIMEOUT.
+#pragma once
+
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
@@ -195,6 +198,7 @@ struct V2<double> {
     double a, b;
     __device__ __forceinline__ V2() {}
     __device__ __forceinline__ V2(double p, double q) : a(p), b(q) {}
+    __device__ __forceinline__ explicit V2(double2 w) : a(w.x), b(w.y) {}
     __device__ __forceinline__ double x() const { return a; }
     __device__ __forceinline__ double y() const { return b; }
 };
@@ -208,42 +212,75 @@ __device__ __forceinline__ V2<double> fma2(V2<double> p, V2<double> q, V2<double
 template <typename T>
 __device__ __forceinline__ V2<T> splat(T a) { return V2<T>(a, a); }
 
+// The constants of the packed arithmetic as (x, x) pairs, passed in
+// parameter space: an f32x2 instruction then takes the pair as one operand
+// instead of a register pair rebuilt from the scalar for every use.
+template <typename T>
+struct PairOf;
+template <>
+struct PairOf<float> { using type = float2; };
+template <>
+struct PairOf<double> { using type = double2; };
+
+template <typename T>
+struct CoefV {
+    using P = typename PairOf<T>::type;
+    P AS, dA, AsAl, A, cL0, dc0, Mt0, Mt1, dC, nq1, q1, q2, dm2, mt, tg, nkt, m6, one, zero;
+};
+
+template <typename T>
+CoefV<T> make_coefv(const Coef<T> &k) {
+    auto p = [](T x) {
+        typename PairOf<T>::type r;
+        r.x = x;
+        r.y = x;
+        return r;
+    };
+    CoefV<T> v;
+    v.AS = p(k.AS); v.dA = p(k.dA); v.AsAl = p(k.AsAl); v.A = p(k.A);
+    v.cL0 = p(k.cL0); v.dc0 = p(k.dc0); v.Mt0 = p(k.Mt0); v.Mt1 = p(k.Mt1);
+    v.dC = p(k.dC); v.nq1 = p(-k.q1); v.q1 = p(k.q1); v.q2 = p(k.q2); v.dm2 = p(k.dm2);
+    v.mt = p(k.mt); v.tg = p(k.tg); v.nkt = p(-k.kt);
+    v.m6 = p(T(-6)); v.one = p(T(1)); v.zero = p(T(0));
+    return v;
+}
+
 // pass A + the centre part of pass B (see pass_a_own) for a pair of cells
 template <typename T, bool EQ>
-__device__ __forceinline__ void pass_a_own2(const Coef<T> &k, V2<T> eS, V2<T> eL, V2<T> c, V2<T> &mu, V2<T> &Mt,
+__device__ __forceinline__ void pass_a_own2(const CoefV<T> &kv, V2<T> eS, V2<T> eL, V2<T> c, V2<T> &mu, V2<T> &Mt,
                                             V2<T> &dmu) {
     const V2<T> S2 = eS * eS;
     const V2<T> s2 = fma2(eL, eL, S2);
     const V2<T> rs(fast_rcp(s2.x()), fast_rcp(s2.y()));
     const V2<T> h = S2 * rs;
-    const V2<T> w = fma2(h, splat(k.dc0), c - splat(k.cL0));
+    const V2<T> w = fma2(h, V2<T>(kv.dc0), c - V2<T>(kv.cL0));
     if (EQ) {
-        mu = splat(k.A) * w;
+        mu = V2<T>(kv.A) * w;
     } else {
-        const V2<T> den = fma2(h, splat(k.dA), splat(k.AS));
-        mu = splat(k.AsAl) * V2<T>(fast_rcp(den.x()), fast_rcp(den.y())) * w;
+        const V2<T> den = fma2(h, V2<T>(kv.dA), V2<T>(kv.AS));
+        mu = V2<T>(kv.AsAl) * V2<T>(fast_rcp(den.x()), fast_rcp(den.y())) * w;
     }
-    Mt = fma2(h, splat(k.Mt1), splat(k.Mt0));
-    const V2<T> D = EQ ? fma2(mu, splat(-k.q1), splat(k.dC))
-                       : splat(k.dC) - mu * fma2(mu, splat(k.q2), splat(k.q1));
-    dmu = splat(k.dm2) * (eS * eL) * (rs * rs) * D;
+    Mt = fma2(h, V2<T>(kv.Mt1), V2<T>(kv.Mt0));
+    const V2<T> D = EQ ? fma2(mu, V2<T>(kv.nq1), V2<T>(kv.dC))
+                       : V2<T>(kv.dC) - mu * fma2(mu, V2<T>(kv.q2), V2<T>(kv.q1));
+    dmu = V2<T>(kv.dm2) * (eS * eL) * (rs * rs) * D;
 }
 
 // pass A alone for a pair (c-only steps)
 template <typename T, bool EQ>
-__device__ __forceinline__ void pass_a2(const Coef<T> &k, V2<T> eS, V2<T> eL, V2<T> c, V2<T> &mu, V2<T> &Mt) {
+__device__ __forceinline__ void pass_a2(const CoefV<T> &kv, V2<T> eS, V2<T> eL, V2<T> c, V2<T> &mu, V2<T> &Mt) {
     const V2<T> S2 = eS * eS;
     const V2<T> s2 = fma2(eL, eL, S2);
     const V2<T> rs(fast_rcp(s2.x()), fast_rcp(s2.y()));
     const V2<T> h = S2 * rs;
-    const V2<T> w = fma2(h, splat(k.dc0), c - splat(k.cL0));
+    const V2<T> w = fma2(h, V2<T>(kv.dc0), c - V2<T>(kv.cL0));
     if (EQ) {
-        mu = splat(k.A) * w;
+        mu = V2<T>(kv.A) * w;
     } else {
-        const V2<T> den = fma2(h, splat(k.dA), splat(k.AS));
-        mu = splat(k.AsAl) * V2<T>(fast_rcp(den.x()), fast_rcp(den.y())) * w;
+        const V2<T> den = fma2(h, V2<T>(kv.dA), V2<T>(kv.AS));
+        mu = V2<T>(kv.AsAl) * V2<T>(fast_rcp(den.x()), fast_rcp(den.y())) * w;
     }
-    Mt = fma2(h, splat(k.Mt1), splat(k.Mt0));
+    Mt = fma2(h, V2<T>(kv.Mt1), V2<T>(kv.Mt0));
 }
 
 // Face ghosts fed by a boundary cell (the BC fill of phasefield.c:1112-1189
@@ -321,10 +358,13 @@ __device__ __forceinline__ Item item_at(int item, int ntiles, int zc, int nz, co
     return it;
 }
 
-template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL, bool MULTI>
+// FULL: every tile of the launch lies inside the domain (nx, ny multiples of
+// the tile), so no cell needs the per-cell "inside the domain" test.
+template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL, bool MULTI, bool FULL>
 __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
-                    const __grid_constant__ CUtensorMap mapC, Geom g1, Coef<T> k, Fields<T> out1, int ntx1, int nty1,
+                    const __grid_constant__ CUtensorMap mapC, Geom g1, Coef<T> k, CoefV<T> kv, Fields<T> out1,
+                    int ntx1, int nty1,
                     int zc1, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
                     int inject_stall, const DomainDesc *__restrict__ table, int ndom, int mitems, int parity) {
     using G = TmaGeo<T>;
@@ -342,6 +382,18 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const int ntiles1 = ntx1 * nty1;
     const int nitems = MULTI ? mitems : ntiles1 * ((g1.nz + zc1 - 1) / zc1);
     const int ob = (ty0 + 1) * BX + tx + XH;          // shared offset of the first own cell
+    static_assert(!(MULTI && FULL), "ensembles take the general path");
+    // the cell of the one-cell ring around the tile that this thread
+    // evaluates (threads < RING): the four edges in turn
+    int ring_o = 0;
+    if (tid < G::RING) {
+        int hx, hy;
+        if (tid < TX) { hx = tid; hy = -1; }
+        else if (tid < 2 * TX) { hx = tid - TX; hy = TY; }
+        else if (tid < 2 * TX + TY) { hx = -1; hy = tid - 2 * TX; }
+        else { hx = TX; hy = tid - 2 * TX - TY; }
+        ring_o = (hy + 1) * BX + hx + XH;
+    }
 
     double acc[3] = {0.0, 0.0, 0.0};
     if ((int)blockIdx.x < nitems) {
@@ -446,9 +498,9 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     Xr.L[i] = V2<T>(rL[o0], rL[o1]);
                     Xr.c[i] = V2<T>(rC[o0], rC[o1]);
                     if (C_ONLY) {
-                        pass_a2<T, EQ>(k, Xr.S[i], Xr.L[i], Xr.c[i], Xr.mu[i], Xr.M[i]);
+                        pass_a2<T, EQ>(kv, Xr.S[i], Xr.L[i], Xr.c[i], Xr.mu[i], Xr.M[i]);
                     } else {
-                        pass_a_own2<T, EQ>(k, Xr.S[i], Xr.L[i], Xr.c[i], Xr.mu[i], Xr.M[i], Xr.d[i]);
+                        pass_a_own2<T, EQ>(kv, Xr.S[i], Xr.L[i], Xr.c[i], Xr.mu[i], Xr.M[i], Xr.d[i]);
                     }
                     wmu[o0] = Xr.mu[i].x();
                     wmu[o1] = Xr.mu[i].y();
@@ -456,16 +508,10 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     wM[o1] = Xr.M[i].y();
                 }
                 if (tid < G::RING) {                   // the one-cell ring around the tile
-                    int hx, hy;
-                    if (tid < TX) { hx = tid; hy = -1; }
-                    else if (tid < 2 * TX) { hx = tid - TX; hy = TY; }
-                    else if (tid < 2 * TX + TY) { hx = -1; hy = tid - 2 * TX; }
-                    else { hx = TX; hy = tid - 2 * TX - TY; }
-                    const int o = (hy + 1) * BX + hx + XH;
                     T mu, M;
-                    (void)pass_a<T, EQ>(k, rS[o], rL[o], rC[o], mu, M);
-                    wmu[o] = mu;
-                    wM[o] = M;
+                    (void)pass_a<T, EQ>(k, rS[ring_o], rL[ring_o], rC[ring_o], mu, M);
+                    wmu[ring_o] = mu;
+                    wM[ring_o] = M;
                 }
                 __syncthreads();
                 if (sm.abort) { dead = true; return false; }
@@ -481,8 +527,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
 #pragma unroll
                     for (int i = 0; i < H; ++i) {
                         const int j0 = i, j1 = i + H;                       // the pair's cells
-                        const bool v0 = vmask & (1u << j0), v1 = vmask & (1u << j1);
-                        if (!(v0 || v1)) continue;
+                        const bool v0 = FULL || (vmask & (1u << j0)), v1 = FULL || (vmask & (1u << j1));
+                        if (!FULL && !(v0 || v1)) continue;
                         const int o0 = ob + j0 * BX, o1 = ob + j1 * BX;
                         const V2<T> mu = Qr.mu[i], M = Qr.M[i], c = Qr.c[i];
                         // y neighbours: pair i-1 / i+1, or a shared row at the column ends
@@ -526,11 +572,11 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                                              V2<T>(nS[o0 - 1], nS[o1 - 1]);
                             const V2<T> L6 = Xr.L[i] + Pr.L[i] + Lyp + Lym + V2<T>(nL[o0 + 1], nL[o1 + 1]) +
                                              V2<T>(nL[o0 - 1], nL[o1 - 1]);
-                            const V2<T> one = splat(T(1)), tg = splat(k.tg), nkt = splat(-k.kt), m6 = splat(T(-6));
+                            const V2<T> one(kv.one), tg(kv.tg), nkt(kv.nkt), m6(kv.m6), mt(kv.mt);
                             const V2<T> S2 = eS * eS, L2 = eL * eL;
                             const V2<T> lapS = fma2(m6, eS, S6), lapL = fma2(m6, eL, L6);
-                            const V2<T> dS = fma2(splat(k.mt) * eS, fma2(tg, L2, S2 - one), fma2(nkt, lapS, eL * dmu));
-                            const V2<T> dL = fma2(splat(k.mt) * eL, fma2(tg, S2, L2 - one), fma2(nkt, lapL, splat(T(0)) - eS * dmu));
+                            const V2<T> dS = fma2(mt * eS, fma2(tg, L2, S2 - one), fma2(nkt, lapS, eL * dmu));
+                            const V2<T> dL = fma2(mt * eL, fma2(tg, S2, L2 - one), fma2(nkt, lapL, V2<T>(kv.zero) - eS * dmu));
                             const V2<T> Sn = eS + dS, Ln = eL + dL;
                             if (v0) {
                                 out.eS[a0] = Sn.x();
@@ -686,11 +732,15 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map) {
 
 template <typename T, bool ST, bool CO, bool EQ, int R>
 static cudaError_t set_attr1() {
-    cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tma_smem_bytes<T>());
+    const int sh = (int)tma_smem_bytes<T>();
+    cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, sh);
     if (e) return e;
-    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)tma_smem_bytes<T>());
+    e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, sh);
+    if (e) return e;
+    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, true, false>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, sh);
 }
 
 template <typename T, int R>
@@ -726,7 +776,7 @@ int tma_grid(const Geom &g, int num_sms, int *zc_out) {
     if (!occ) {
         if (set_attrs<T>() != cudaSuccess) return -1;
         int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 3, false>, G::NT,
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 1, false, false>, G::NT,
                                                           tma_smem_bytes<T>()) != cudaSuccess || o < 1)
             o = 1;
         occ = o;
@@ -769,7 +819,7 @@ int tma_grid_for_zc(const Geom &g, int num_sms, int zc) {
     int dummy = 0;
     if (tma_grid<T>(g, num_sms, &dummy) < 1) return -1;    // attributes + occupancy
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 3, false>, G::NT,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 1, false, false>, G::NT,
                                                       tma_smem_bytes<T>()) != cudaSuccess || occ < 1)
         occ = 1;
     const int64_t ntiles = (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY);
@@ -781,7 +831,7 @@ int tma_grid_for_zc(const Geom &g, int num_sms, int zc) {
     return (int)(items < slots ? items : slots);
 }
 
-template <typename T, int R>
+template <typename T, int R, bool FULL>
 static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only, bool eqA,
                      double *partials, int grid, int zc, int *err, unsigned long long limit_ns, int inject_stall,
                      cudaStream_t s) {
@@ -789,10 +839,11 @@ static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, F
     const int ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
     const size_t sh = tma_smem_bytes<T>();
     const bool st = partials != nullptr;
-#define PPF_LAUNCH(ST, CO, EQ)                                                                                      \
-    step_tma_kernel<T, ST, CO, EQ, R, false><<<grid, G::NT, sh, s>>>(maps[0], maps[1], maps[2], g, k, out, ntx, nty,  \
-                                                                     zc, partials, err, limit_ns, inject_stall,     \
-                                                                     nullptr, 0, 0, 0)
+    const CoefV<T> kv = make_coefv(k);
+#define PPF_LAUNCH(ST, CO, EQ)                                                                                   \
+    step_tma_kernel<T, ST, CO, EQ, R, false, FULL><<<grid, G::NT, sh, s>>>(                                     \
+        maps[0], maps[1], maps[2], g, k, kv, out, ntx, nty, zc, partials, err, limit_ns, inject_stall, nullptr, 0, \
+        0, 0)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -807,10 +858,19 @@ template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
                             bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
                             int inject_stall, cudaStream_t s) {
-    if (tune.roll == 1)
-        launch_r<T, 1>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns, inject_stall, s);
-    else
-        launch_r<T, 3>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns, inject_stall, s);
+    using G = TmaGeo<T>;
+    const bool full = g.nx % G::TX == 0 && g.ny % G::TY == 0;
+    if (tune.roll == 1) {
+        if (full) launch_r<T, 1, true>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns,
+                                       inject_stall, s);
+        else launch_r<T, 1, false>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns,
+                                   inject_stall, s);
+    } else {
+        if (full) launch_r<T, 3, true>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns,
+                                       inject_stall, s);
+        else launch_r<T, 3, false>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns,
+                                   inject_stall, s);
+    }
     return cudaGetLastError();
 }
 
@@ -826,9 +886,11 @@ static void launch_multi_r(const DomainDesc *table, int ndom, int items, const C
     Geom g0;
     memset(&g0, 0, sizeof g0);
     const Fields<T> o0 = {nullptr, nullptr, nullptr};
-#define PPF_LAUNCH(ST, CO, EQ)                                                                                 \
-    step_tma_kernel<T, ST, CO, EQ, R, true><<<grid, G::NT, sh, s>>>(none, none, none, g0, k, o0, 1, 1, 1, partials, \
-                                                                    err, limit_ns, 0, table, ndom, items, parity)
+    const CoefV<T> kv = make_coefv(k);
+#define PPF_LAUNCH(ST, CO, EQ)                                                                                       \
+    step_tma_kernel<T, ST, CO, EQ, R, true, false><<<grid, G::NT, sh, s>>>(none, none, none, g0, k, kv, o0, 1, 1, 1, \
+                                                                           partials, err, limit_ns, 0, table, ndom, \
+                                                                           items, parity)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -862,33 +924,12 @@ int tma_grid_items(int64_t items, int num_sms) {
     int zc = 1;
     if (tma_grid<T>(g, num_sms, &zc) < 1) return -1;     // attributes + occupancy
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 3, true>,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 1, true, false>,
                                                       TmaGeo<T>::NT, tma_smem_bytes<T>()) != cudaSuccess ||
         occ < 1)
         occ = 1;
     const int64_t slots = (int64_t)occ * num_sms;
     return (int)(items < slots ? items : slots);
 }
-
-template void step_tile<float>(int *, int *);
-template void step_tile<double>(int *, int *);
-template int tma_grid_items<float>(int64_t, int);
-template int tma_grid_items<double>(int64_t, int);
-template cudaError_t launch_step_multi<float>(const DomainDesc *, int, int, const Coef<float> &, bool, bool, int,
-                                              double *, int, int, int *, unsigned long long, cudaStream_t);
-template cudaError_t launch_step_multi<double>(const DomainDesc *, int, int, const Coef<double> &, bool, bool, int,
-                                               double *, int, int, int *, unsigned long long, cudaStream_t);
-template int make_field_map<float>(const Geom &, const float *, CUtensorMap *);
-template int make_field_map<double>(const Geom &, const double *, CUtensorMap *);
-template int tma_grid<float>(const Geom &, int, int *);
-template int tma_grid<double>(const Geom &, int, int *);
-template int tma_grid_for_zc<float>(const Geom &, int, int);
-template int tma_grid_for_zc<double>(const Geom &, int, int);
-template cudaError_t launch_step_tma<float>(const Geom &, const Coef<float> &, const CUtensorMap *, Fields<float>,
-                                            bool, bool, double *, const StepTune &, int *, unsigned long long, int,
-                                            cudaStream_t);
-template cudaError_t launch_step_tma<double>(const Geom &, const Coef<double> &, const CUtensorMap *,
-                                             Fields<double>, bool, bool, double *, const StepTune &, int *,
-                                             unsigned long long, int, cudaStream_t);
 
 }  // namespace ppf

@@ -1,4 +1,4 @@
-// ppf_step_tma.h -- launcher of the TMA-fed fused step (ppf_step_tma.cu).
+// ppf_step_tma.h -- launcher of the TMA-fed fused step (ppf_step_tma.cuh).
 #pragma once
 
 #include <cuda.h>

@@ -524,11 +524,17 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     const bool zface = q == 0 || q == g.nz - 1;
                     const unsigned gm = vmask & (zface ? ~0u : emask);   // own cells that feed ghosts
                     const int64_t base = col + (int64_t)(q + 1) * g.PS;
+                    // the new values of the plane's own cells, kept for the face
+                    // ghosts below (staged only when this thread feeds any)
+                    V2<T> gS[H], gL[H], gC[H];
 #pragma unroll
                     for (int i = 0; i < H; ++i) {
                         const int j0 = i, j1 = i + H;                       // the pair's cells
                         const bool v0 = FULL || (vmask & (1u << j0)), v1 = FULL || (vmask & (1u << j1));
-                        if (!FULL && !(v0 || v1)) continue;
+                        if (!FULL && !(v0 || v1)) {
+                            gS[i] = gL[i] = gC[i] = splat(T(0));   // outside: never feeds a ghost
+                            continue;
+                        }
                         const int o0 = ob + j0 * BX, o1 = ob + j1 * BX;
                         const V2<T> mu = Qr.mu[i], M = Qr.M[i], c = Qr.c[i];
                         // y neighbours: pair i-1 / i+1, or a shared row at the column ends
@@ -552,8 +558,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                         if (C_ONLY) {
                             if (v0) out.c[a0] = cn.x();
                             if (v1) out.c[a1] = cn.y();
-                            if (gm & (1u << j0)) sm.gstage[tid][j0][2] = cn.x();
-                            if (gm & (1u << j1)) sm.gstage[tid][j1][2] = cn.y();
+                            gS[i] = gL[i] = splat(T(0));
+                            gC[i] = cn;
                             if (STATS) {
                                 if (v0) acc[0] += (double)fl.x() * (double)fl.x();
                                 if (v1) acc[0] += (double)fl.y() * (double)fl.y();
@@ -588,16 +594,9 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                                 out.eL[a1] = Ln.y();
                                 out.c[a1] = cn.y();
                             }
-                            if (gm & (1u << j0)) {
-                                sm.gstage[tid][j0][0] = Sn.x();
-                                sm.gstage[tid][j0][1] = Ln.x();
-                                sm.gstage[tid][j0][2] = cn.x();
-                            }
-                            if (gm & (1u << j1)) {
-                                sm.gstage[tid][j1][0] = Sn.y();
-                                sm.gstage[tid][j1][1] = Ln.y();
-                                sm.gstage[tid][j1][2] = cn.y();
-                            }
+                            gS[i] = Sn;
+                            gL[i] = Ln;
+                            gC[i] = cn;
                             if (STATS) {
                                 if (v0) {
                                     acc[0] += (double)fl.x() * (double)fl.x();
@@ -612,10 +611,16 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             }
                         }
                     }
-                    // face ghosts of this thread's boundary cells, from the values
-                    // staged in shared memory above: one compact loop instead of a
+                    // face ghosts of this thread's boundary cells: the kept values
+                    // staged in shared memory, then one compact loop instead of a
                     // copy of the ghost code per cell
                     if (gm) {
+#pragma unroll
+                        for (int i = 0; i < H; ++i) {
+                            T *a = sm.gstage[tid][i], *b = sm.gstage[tid][i + H];
+                            a[0] = gS[i].x(); a[1] = gL[i].x(); a[2] = gC[i].x();
+                            b[0] = gS[i].y(); b[1] = gL[i].y(); b[2] = gC[i].y();
+                        }
 #pragma unroll 1
                         for (int j = 0; j < CY; ++j) {
                             if (!(gm & (1u << j))) continue;

@@ -135,6 +135,22 @@ def test_fp32_against_fp64_oracle_64cubed():
     assert abs(g["solid"] - o["solid"]) <= 1e-6 * o["solid"]
 
 
+@pytest.mark.parametrize("shape", [(16, 32, 64), (17, 33, 70)])
+@pytest.mark.parametrize("bc", [0, 1])
+def test_fp32_full_and_partial_tiles_against_fp64_oracle(shape, bc):
+    """The FP32 step on a domain whose tiles all lie inside (nx, ny multiples
+    of 64 and 16: the launch without per-cell domain tests) and on one with
+    partial tiles, 100 steps at dt = 0.8 of the limit, against the FP64
+    oracle: max-abs field error <= 2e-5 (as for 64^3), mass to 1e-6."""
+    st = smooth_state(shape, seed=21 + bc)
+    (gS, gL, gc), g = run_gpu(st, 100, bc=bc, precision="f32", dt=DT08)
+    oS, oL, oc, _ = oracle.run(*st, 100, bc=bc, params=oracle.reference_params(dt=DT08))
+    errs = [maxabs(gS, oS), maxabs(gL, oL), maxabs(gc, oc)]
+    assert max(errs) <= 2e-5, errs
+    o = oracle.observe(oS, oL, oc, bc=bc)
+    assert abs(g["mass"] - o["mass"]) <= 1e-6 * abs(o["mass"])
+
+
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 def test_solute_conserved_at_256cubed(precision):
     """Sum c is conserved by the flux form (phasefield.c:374-384): FP64 to

@@ -30,6 +30,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 #include "ppf_internal.h"
 #include "ppf_step_tma.h"
@@ -69,7 +70,6 @@ struct alignas(128) TmaSmem {
     T mm[3][2][G::BOX];           // mu, M of three consecutive planes
     T gstage[G::NT][G::CY][3];    // new values of a thread's boundary cells, for their ghosts
     unsigned long long bar[G::S];
-    int abort;
 };
 
 template <typename T>
@@ -288,8 +288,8 @@ __device__ __forceinline__ void pass_a2(const CoefV<T> &kv, V2<T> eS, V2<T> eL, 
 // is copied to ghost n (periodic) or -1 (no-flux), cell n-1 to ghost -1
 // (periodic) or n (no-flux).  `a` is the cell's own storage index; each
 // ghost is an offset from it.
-template <typename T, bool C_ONLY>
-__device__ __forceinline__ void put_ghost(const Fields<T> &o, int64_t a, T s, T l, T c) {
+template <typename T, bool C_ONLY, typename I = int64_t>
+__device__ __forceinline__ void put_ghost(const Fields<T> &o, I a, T s, T l, T c) {
     if (!C_ONLY) {
         o.eS[a] = s;
         o.eL[a] = l;
@@ -399,7 +399,6 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     if ((int)blockIdx.x < nitems) {
         if (tid == 0) {
             for (int s = 0; s < S; ++s) mbar_init(smem_u32(&sm.bar[s]), 1);
-            sm.abort = 0;
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
@@ -485,10 +484,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             // from (Pr = pz-2, Qr = pz-1, Xr = pz); false once the item is done
             auto plane = [&](int pz, PlaneRegs<T, H> &Pr, PlaneRegs<T, H> &Qr, PlaneRegs<T, H> &Xr) -> bool {
                 if (pz > z1) return false;
-                if (!mbar_wait(smem_u32(&sm.bar[st]), par, limit_ns)) {
-                    sm.abort = 1;
-                    atomicOr(err, 1);
-                }
+                const bool late = !mbar_wait(smem_u32(&sm.bar[st]), par, limit_ns);
+                if (late) atomicOr(err, 1);
                 const T *rS = sm.raw[st][0], *rL = sm.raw[st][1], *rC = sm.raw[st][2];
                 T *wmu = sm.mm[mb][0], *wM = sm.mm[mb][1];
 #pragma unroll
@@ -513,8 +510,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     wmu[ring_o] = mu;
                     wM[ring_o] = M;
                 }
-                __syncthreads();
-                if (sm.abort) { dead = true; return false; }
+                // the plane barrier also tells every thread whether any wait ran out
+                if (__syncthreads_or(late)) { dead = true; return false; }
                 if (tid == 0 && p_item < nitems) issue();   // refill the stage freed two planes ago
 
                 const int q = pz - 1;
@@ -523,7 +520,10 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     const T *nmu = sm.mm[mb_prev][0], *nM = sm.mm[mb_prev][1];
                     const bool zface = q == 0 || q == g.nz - 1;
                     const unsigned gm = vmask & (zface ? ~0u : emask);   // own cells that feed ghosts
-                    const int64_t base = col + (int64_t)(q + 1) * g.PS;
+                    // FULL launches address the state with 32-bit element offsets (the
+                    // host takes that variant only when every offset fits)
+                    using Off = typename std::conditional<FULL, uint32_t, int64_t>::type;
+                    const Off base = (Off)col + (Off)(q + 1) * (Off)g.PS;
                     // the new values of the plane's own cells, kept for the face
                     // ghosts below (staged only when this thread feeds any)
                     V2<T> gS[H], gL[H], gC[H];
@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                         fl = fma2(Mxp + M, muxp - mu, fl);
                         fl = fma2(Mxm + M, muxm - mu, fl);
                         const V2<T> cn = c + fl;
-                        const int64_t a0 = base + (int64_t)j0 * g.P, a1 = base + (int64_t)j1 * g.P;
+                        const Off a0 = base + (Off)j0 * (Off)g.P, a1 = base + (Off)j1 * (Off)g.P;
                         if (C_ONLY) {
                             if (v0) out.c[a0] = cn.x();
                             if (v1) out.c[a1] = cn.y();
@@ -611,10 +611,47 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             }
                         }
                     }
-                    // face ghosts of this thread's boundary cells: the kept values
-                    // staged in shared memory, then one compact loop instead of a
-                    // copy of the ghost code per cell
-                    if (gm) {
+                    if constexpr (FULL) {
+                        // face ghosts straight from the kept values.  Every tile lies
+                        // inside the domain, so an x face is a whole thread column, a y
+                        // face the first or last own row of a thread, a z face a plane.
+                        // Periodic: cell 0 feeds ghost n, cell n-1 ghost -1; no-flux:
+                        // cell 0 feeds ghost -1, cell n-1 ghost n.
+                        const bool per = g.bc == 0;
+                        auto put_pair = [&](int i, Off d) {
+                            put_ghost<T, C_ONLY, Off>(out, base + (Off)i * (Off)g.P + d, gS[i].x(), gL[i].x(), gC[i].x());
+                            put_ghost<T, C_ONLY, Off>(out, base + (Off)(i + H) * (Off)g.P + d, gS[i].y(), gL[i].y(),
+                                                      gC[i].y());
+                        };
+                        if (X == 0 || X == g.nx - 1) {
+                            const Off d = X == 0 ? (per ? (Off)g.nx : (Off)-1) : (per ? (Off)-g.nx : (Off)1);
+#pragma unroll
+                            for (int i = 0; i < H; ++i) put_pair(i, d);
+                        }
+                        const int Yf = y0 + ty0;
+                        if (Yf == 0) {
+                            const Off d = per ? (Off)g.ny * (Off)g.P : (Off)-g.P;
+                            put_ghost<T, C_ONLY, Off>(out, base + d, gS[0].x(), gL[0].x(), gC[0].x());
+                        }
+                        if (Yf + CY == g.ny) {
+                            const Off d = per ? (Off)(-g.ny) * (Off)g.P : (Off)g.P;
+                            put_ghost<T, C_ONLY, Off>(out, base + (Off)(CY - 1) * (Off)g.P + d, gS[H - 1].y(),
+                                                      gL[H - 1].y(), gC[H - 1].y());
+                        }
+                        if (q == 0) {
+                            const Off d = per ? (Off)g.nz * (Off)g.PS : (Off)-g.PS;
+#pragma unroll
+                            for (int i = 0; i < H; ++i) put_pair(i, d);
+                        }
+                        if (q == g.nz - 1) {
+                            const Off d = per ? (Off)(-g.nz) * (Off)g.PS : (Off)g.PS;
+#pragma unroll
+                            for (int i = 0; i < H; ++i) put_pair(i, d);
+                        }
+                    } else if (gm) {
+                        // face ghosts of this thread's boundary cells: the kept values
+                        // staged in shared memory, then one compact loop instead of a
+                        // copy of the ghost code per cell
 #pragma unroll
                         for (int i = 0; i < H; ++i) {
                             T *a = sm.gstage[tid][i], *b = sm.gstage[tid][i + H];
@@ -864,7 +901,8 @@ cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *
                             bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
                             int inject_stall, cudaStream_t s) {
     using G = TmaGeo<T>;
-    const bool full = g.nx % G::TX == 0 && g.ny % G::TY == 0;
+    // FULL: every tile inside the domain, and every element offset below 2^32
+    const bool full = g.nx % G::TX == 0 && g.ny % G::TY == 0 && g.total <= ((int64_t)1 << 32);
     if (tune.roll == 1) {
         if (full) launch_r<T, 1, true>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns,
                                        inject_stall, s);

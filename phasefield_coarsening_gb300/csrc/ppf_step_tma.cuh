@@ -41,7 +41,8 @@ template <typename T>
 struct TmaCfg;
 template <>
 struct TmaCfg<float> {
-    static constexpr int TX = 64, TY = 16, NT = 256, S = 4, XH = 4;
+    // S = 5: three planes in flight; two CTAs of 256 threads fit an SM
+    static constexpr int TX = 64, TY = 16, NT = 256, S = 5, XH = 4;
 };
 template <>
 struct TmaCfg<double> {
@@ -59,7 +60,7 @@ struct TmaGeo {
     static constexpr int WX = TX / 32, WY = (NT / 32) / WX, CY = TY / WY;
     static constexpr int RING = 2 * TX + 2 * TY;
     static_assert(TX % 32 == 0 && (NT / 32) % WX == 0 && TY % WY == 0, "tile/warp mismatch");
-    static_assert(RING <= NT, "one ring position per thread");
+    static_assert(RING / 2 <= NT, "one ring pair per thread");
     static_assert(BX * sizeof(T) % 16 == 0 && (XH * sizeof(T)) % 16 == 0, "TMA box alignment");
 };
 
@@ -68,7 +69,6 @@ struct alignas(128) TmaSmem {
     using G = TmaGeo<T>;
     T raw[G::S][3][G::BOX_PAD];   // etaS, etaL, c boxes per stage
     T mm[3][2][G::BOX];           // mu, M of three consecutive planes
-    T gstage[G::NT][G::CY][3];    // new values of a thread's boundary cells, for their ghosts
     unsigned long long bar[G::S];
 };
 
@@ -283,11 +283,9 @@ __device__ __forceinline__ void pass_a2(const CoefV<T> &kv, V2<T> eS, V2<T> eL, 
     Mt = fma2(h, V2<T>(kv.Mt1), V2<T>(kv.Mt0));
 }
 
-// Face ghosts fed by a boundary cell (the BC fill of phasefield.c:1112-1189
-// applied to the new state): along an axis of n cells and stride st, cell 0
-// is copied to ghost n (periodic) or -1 (no-flux), cell n-1 to ghost -1
-// (periodic) or n (no-flux).  `a` is the cell's own storage index; each
-// ghost is an offset from it.
+// One face ghost cell at storage index `a` (the BC fill of
+// phasefield.c:1112-1189 applied to the new state; the caller picks the
+// ghost that each boundary cell feeds).
 template <typename T, bool C_ONLY, typename I = int64_t>
 __device__ __forceinline__ void put_ghost(const Fields<T> &o, I a, T s, T l, T c) {
     if (!C_ONLY) {
@@ -295,19 +293,6 @@ __device__ __forceinline__ void put_ghost(const Fields<T> &o, I a, T s, T l, T c
         o.eL[a] = l;
     }
     o.c[a] = c;
-}
-
-template <typename T, bool C_ONLY>
-__device__ __forceinline__ void store_ghosts(const Geom &g, const Fields<T> &o, int64_t a, int x, int y, int z, T s,
-                                             T l, T c) {
-    const int idx[3] = {x, y, z};
-    const int n[3] = {g.nx, g.ny, g.nz};
-    const int64_t st[3] = {1, g.P, g.PS};
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        if (idx[d] == 0) put_ghost<T, C_ONLY>(o, a + (g.bc == 0 ? (int64_t)n[d] : (int64_t)-1) * st[d], s, l, c);
-        if (idx[d] == n[d] - 1) put_ghost<T, C_ONLY>(o, a + (g.bc == 0 ? -(int64_t)n[d] : (int64_t)1) * st[d], s, l, c);
-    }
 }
 
 // Work items are (z chunk, x-y tile) pairs in chunk-major order, dealt
@@ -383,16 +368,22 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const int nitems = MULTI ? mitems : ntiles1 * ((g1.nz + zc1 - 1) / zc1);
     const int ob = (ty0 + 1) * BX + tx + XH;          // shared offset of the first own cell
     static_assert(!(MULTI && FULL), "ensembles take the general path");
-    // the cell of the one-cell ring around the tile that this thread
-    // evaluates (threads < RING): the four edges in turn
-    int ring_o = 0;
-    if (tid < G::RING) {
-        int hx, hy;
-        if (tid < TX) { hx = tid; hy = -1; }
-        else if (tid < 2 * TX) { hx = tid - TX; hy = TY; }
-        else if (tid < 2 * TX + TY) { hx = -1; hy = tid - 2 * TX; }
-        else { hx = TX; hy = tid - 2 * TX - TY; }
-        ring_o = (hy + 1) * BX + hx + XH;
+    // the pair of cells of the one-cell ring around the tile that this thread
+    // evaluates: the last RING/2 threads (warp 0 also feeds the TMA ring), each
+    // a cell of the top row with the one below it in the bottom row, or a cell
+    // of the left column with the one beside it in the right column
+    constexpr int RP = G::RING / 2;
+    const bool ring = tid >= G::NT - RP;
+    int ring_o0 = 0, ring_o1 = 0;
+    if (ring) {
+        const int r = tid - (G::NT - RP);
+        if (r < TX) {
+            ring_o0 = XH + r;                               // (r, -1)
+            ring_o1 = (TY + 1) * BX + XH + r;               // (r, TY)
+        } else {
+            ring_o0 = (r - TX + 1) * BX + XH - 1;           // (-1, r - TX)
+            ring_o1 = (r - TX + 1) * BX + XH + TX;          // (TX, r - TX)
+        }
     }
 
     double acc[3] = {0.0, 0.0, 0.0};
@@ -470,13 +461,12 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             const int bx = it.tile % ntx, by = it.tile / ntx;
             const int x0 = bx * TX, y0 = by * TY, z0 = it.z0, z1 = it.z1;
             const int X = x0 + tx;
-            // per own row j: inside the domain (bit j of vmask), on an x or y face (bit j of emask)
-            unsigned vmask = 0, emask = 0;
+            // per own row j: inside the domain (bit j of vmask)
+            unsigned vmask = 0;
 #pragma unroll
             for (int j = 0; j < CY; ++j) {
                 const int Y = y0 + ty0 + j;
                 if (X < g.nx && Y < g.ny) vmask |= 1u << j;
-                if (X == 0 || X == g.nx - 1 || Y == 0 || Y == g.ny - 1) emask |= 1u << j;
             }
             const int64_t col = (int64_t)(y0 + ty0 + 1) * g.P + X + g.xoff;   // storage of own cell j=0, z=-1
 
@@ -504,11 +494,14 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     wM[o0] = Xr.M[i].x();
                     wM[o1] = Xr.M[i].y();
                 }
-                if (tid < G::RING) {                   // the one-cell ring around the tile
-                    T mu, M;
-                    (void)pass_a<T, EQ>(k, rS[ring_o], rL[ring_o], rC[ring_o], mu, M);
-                    wmu[ring_o] = mu;
-                    wM[ring_o] = M;
+                if (ring) {                            // the one-cell ring around the tile
+                    V2<T> mu, M;
+                    pass_a2<T, EQ>(kv, V2<T>(rS[ring_o0], rS[ring_o1]), V2<T>(rL[ring_o0], rL[ring_o1]),
+                                   V2<T>(rC[ring_o0], rC[ring_o1]), mu, M);
+                    wmu[ring_o0] = mu.x();
+                    wmu[ring_o1] = mu.y();
+                    wM[ring_o0] = M.x();
+                    wM[ring_o1] = M.y();
                 }
                 // the plane barrier also tells every thread whether any wait ran out
                 if (__syncthreads_or(late)) { dead = true; return false; }
@@ -518,14 +511,11 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 if (q >= z0) {
                     const T *nS = sm.raw[st_prev][0], *nL = sm.raw[st_prev][1];
                     const T *nmu = sm.mm[mb_prev][0], *nM = sm.mm[mb_prev][1];
-                    const bool zface = q == 0 || q == g.nz - 1;
-                    const unsigned gm = vmask & (zface ? ~0u : emask);   // own cells that feed ghosts
                     // FULL launches address the state with 32-bit element offsets (the
                     // host takes that variant only when every offset fits)
                     using Off = typename std::conditional<FULL, uint32_t, int64_t>::type;
                     const Off base = (Off)col + (Off)(q + 1) * (Off)g.PS;
-                    // the new values of the plane's own cells, kept for the face
-                    // ghosts below (staged only when this thread feeds any)
+                    // the new values of the plane's own cells, kept for the face ghosts below
                     V2<T> gS[H], gL[H], gC[H];
 #pragma unroll
                     for (int i = 0; i < H; ++i) {
@@ -611,59 +601,48 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             }
                         }
                     }
-                    if constexpr (FULL) {
-                        // face ghosts straight from the kept values.  Every tile lies
-                        // inside the domain, so an x face is a whole thread column, a y
-                        // face the first or last own row of a thread, a z face a plane.
+                    {
+                        // face ghosts straight from the kept values.  An x face is a
+                        // whole thread column, a y face one own row of a thread, a z face
+                        // a plane; cells outside the domain (partial tiles) feed none.
                         // Periodic: cell 0 feeds ghost n, cell n-1 ghost -1; no-flux:
                         // cell 0 feeds ghost -1, cell n-1 ghost n.
                         const bool per = g.bc == 0;
-                        auto put_pair = [&](int i, Off d) {
-                            put_ghost<T, C_ONLY, Off>(out, base + (Off)i * (Off)g.P + d, gS[i].x(), gL[i].x(), gC[i].x());
-                            put_ghost<T, C_ONLY, Off>(out, base + (Off)(i + H) * (Off)g.P + d, gS[i].y(), gL[i].y(),
-                                                      gC[i].y());
-                        };
-                        if (X == 0 || X == g.nx - 1) {
-                            const Off d = X == 0 ? (per ? (Off)g.nx : (Off)-1) : (per ? (Off)-g.nx : (Off)1);
-#pragma unroll
-                            for (int i = 0; i < H; ++i) put_pair(i, d);
-                        }
                         const int Yf = y0 + ty0;
-                        if (Yf == 0) {
-                            const Off d = per ? (Off)g.ny * (Off)g.P : (Off)-g.P;
-                            put_ghost<T, C_ONLY, Off>(out, base + d, gS[0].x(), gL[0].x(), gC[0].x());
+                        auto put_row = [&](int j, Off d) {    // own row j (a constant once unrolled)
+                            if (!FULL && !(vmask & (1u << j))) return;
+                            const Off a = base + (Off)j * (Off)g.P + d;
+                            if (j < H) put_ghost<T, C_ONLY, Off>(out, a, gS[j].x(), gL[j].x(), gC[j].x());
+                            else put_ghost<T, C_ONLY, Off>(out, a, gS[j - H].y(), gL[j - H].y(), gC[j - H].y());
+                        };
+                        // (a one-cell-wide domain feeds both x ghosts from the same cell)
+                        if (X == 0) {
+                            const Off d = per ? (Off)g.nx : (Off)-1;
+#pragma unroll
+                            for (int j = 0; j < CY; ++j) put_row(j, d);
                         }
-                        if (Yf + CY == g.ny) {
-                            const Off d = per ? (Off)(-g.ny) * (Off)g.P : (Off)g.P;
-                            put_ghost<T, C_ONLY, Off>(out, base + (Off)(CY - 1) * (Off)g.P + d, gS[H - 1].y(),
-                                                      gL[H - 1].y(), gC[H - 1].y());
+                        if (X == g.nx - 1) {
+                            const Off d = per ? (Off)-g.nx : (Off)1;
+#pragma unroll
+                            for (int j = 0; j < CY; ++j) put_row(j, d);
+                        }
+#pragma unroll
+                        for (int j = 0; j < CY; ++j) {
+                            // with whole tiles a y face row is a thread's first or last
+                            if (FULL ? (j == 0 && Yf == 0) : (Yf + j == 0))
+                                put_row(j, per ? (Off)g.ny * (Off)g.P : (Off)-g.P);
+                            if (FULL ? (j == CY - 1 && Yf + CY == g.ny) : (Yf + j == g.ny - 1))
+                                put_row(j, per ? (Off)(-g.ny) * (Off)g.P : (Off)g.P);
                         }
                         if (q == 0) {
                             const Off d = per ? (Off)g.nz * (Off)g.PS : (Off)-g.PS;
 #pragma unroll
-                            for (int i = 0; i < H; ++i) put_pair(i, d);
+                            for (int j = 0; j < CY; ++j) put_row(j, d);
                         }
                         if (q == g.nz - 1) {
                             const Off d = per ? (Off)(-g.nz) * (Off)g.PS : (Off)g.PS;
 #pragma unroll
-                            for (int i = 0; i < H; ++i) put_pair(i, d);
-                        }
-                    } else if (gm) {
-                        // face ghosts of this thread's boundary cells: the kept values
-                        // staged in shared memory, then one compact loop instead of a
-                        // copy of the ghost code per cell
-#pragma unroll
-                        for (int i = 0; i < H; ++i) {
-                            T *a = sm.gstage[tid][i], *b = sm.gstage[tid][i + H];
-                            a[0] = gS[i].x(); a[1] = gL[i].x(); a[2] = gC[i].x();
-                            b[0] = gS[i].y(); b[1] = gL[i].y(); b[2] = gC[i].y();
-                        }
-#pragma unroll 1
-                        for (int j = 0; j < CY; ++j) {
-                            if (!(gm & (1u << j))) continue;
-                            const int64_t a = base + (int64_t)j * g.P;
-                            store_ghosts<T, C_ONLY>(g, out, a, X, y0 + ty0 + j, q, sm.gstage[tid][j][0],
-                                                    sm.gstage[tid][j][1], sm.gstage[tid][j][2]);
+                            for (int j = 0; j < CY; ++j) put_row(j, d);
                         }
                     }
                 }

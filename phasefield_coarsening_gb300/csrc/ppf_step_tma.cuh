@@ -68,7 +68,7 @@ template <typename T>
 struct alignas(128) TmaSmem {
     using G = TmaGeo<T>;
     T raw[G::S][3][G::BOX_PAD];   // etaS, etaL, c boxes per stage
-    T mm[3][2][G::BOX];           // mu, M of three consecutive planes
+    T mm[3][2][G::BOX];           // mu, M of three consecutive planes (MmLay)
     unsigned long long bar[G::S];
 };
 
@@ -211,6 +211,33 @@ __device__ __forceinline__ V2<double> fma2(V2<double> p, V2<double> q, V2<double
 
 template <typename T>
 __device__ __forceinline__ V2<T> splat(T a) { return V2<T>(a, a); }
+
+// a pair stored as two adjacent elements (one 2-element shared access)
+__device__ __forceinline__ V2<float> ld2(const float *p) { return V2<float>(*reinterpret_cast<const float2 *>(p)); }
+__device__ __forceinline__ V2<double> ld2(const double *p) { return V2<double>(*reinterpret_cast<const double2 *>(p)); }
+__device__ __forceinline__ void st2(float *p, V2<float> v) { *reinterpret_cast<float2 *>(p) = v.v; }
+__device__ __forceinline__ void st2(double *p, V2<double> v) { *reinterpret_cast<double2 *>(p) = make_double2(v.a, v.b); }
+
+// Layout of one mu or M plane in shared memory (BOX elements): the TY rows
+// of the tile as TY/2 pair rows -- pair row wy*H + i interleaves, element by
+// element, the rows ty0 + i and ty0 + i + H of warp row wy, so that a
+// thread's pair of cells and the pairs beside it in x are one 2-element
+// access each -- then the ring rows -1 and TY as plain rows.  Column c of
+// every row holds x = c - XH.
+template <typename T>
+struct MmLay {
+    using G = TmaGeo<T>;
+    static constexpr int H = G::CY / 2;
+    static constexpr int TOP = G::TY * G::BX, BOT = TOP + G::BX;
+    static_assert(BOT + G::BX == G::BOX, "mu/M plane size");
+    __device__ static int pair(int pr, int col) { return (pr * G::BX + col) * 2; }
+    __device__ static int row(int r, int col) {   // element of tile row r in [-1, TY]
+        if (r < 0) return TOP + col;
+        if (r >= G::TY) return BOT + col;
+        const int w = r % G::CY;
+        return pair((r / G::CY) * H + w % H, col) + w / H;
+    }
+};
 
 // The constants of the packed arithmetic as (x, x) pairs, passed in
 // parameter space: an f32x2 instruction then takes the pair as one operand
@@ -374,17 +401,24 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     // of the left column with the one beside it in the right column
     constexpr int RP = G::RING / 2;
     const bool ring = tid >= G::NT - RP;
-    int ring_o0 = 0, ring_o1 = 0;
+    int ring_o0 = 0, ring_o1 = 0, ring_m0 = 0, ring_m1 = 0;   // in the TMA box / the mu-M plane
     if (ring) {
         const int r = tid - (G::NT - RP);
         if (r < TX) {
             ring_o0 = XH + r;                               // (r, -1)
             ring_o1 = (TY + 1) * BX + XH + r;               // (r, TY)
+            ring_m0 = MmLay<T>::row(-1, XH + r);
+            ring_m1 = MmLay<T>::row(TY, XH + r);
         } else {
             ring_o0 = (r - TX + 1) * BX + XH - 1;           // (-1, r - TX)
             ring_o1 = (r - TX + 1) * BX + XH + TX;          // (TX, r - TX)
+            ring_m0 = MmLay<T>::row(r - TX, XH - 1);
+            ring_m1 = MmLay<T>::row(r - TX, XH + TX);
         }
     }
+    // the thread's first pair in a mu/M plane, and its rows above and below
+    const int pofs = MmLay<T>::pair((warp / G::WX) * (CY / 2), tx + XH);
+    const int m_above = MmLay<T>::row(ty0 - 1, tx + XH), m_below = MmLay<T>::row(ty0 + CY, tx + XH);
 
     double acc[3] = {0.0, 0.0, 0.0};
     if ((int)blockIdx.x < nitems) {
@@ -489,19 +523,17 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     } else {
                         pass_a_own2<T, EQ>(kv, Xr.S[i], Xr.L[i], Xr.c[i], Xr.mu[i], Xr.M[i], Xr.d[i]);
                     }
-                    wmu[o0] = Xr.mu[i].x();
-                    wmu[o1] = Xr.mu[i].y();
-                    wM[o0] = Xr.M[i].x();
-                    wM[o1] = Xr.M[i].y();
+                    st2(wmu + pofs + 2 * BX * i, Xr.mu[i]);
+                    st2(wM + pofs + 2 * BX * i, Xr.M[i]);
                 }
                 if (ring) {                            // the one-cell ring around the tile
                     V2<T> mu, M;
                     pass_a2<T, EQ>(kv, V2<T>(rS[ring_o0], rS[ring_o1]), V2<T>(rL[ring_o0], rL[ring_o1]),
                                    V2<T>(rC[ring_o0], rC[ring_o1]), mu, M);
-                    wmu[ring_o0] = mu.x();
-                    wmu[ring_o1] = mu.y();
-                    wM[ring_o0] = M.x();
-                    wM[ring_o1] = M.y();
+                    wmu[ring_m0] = mu.x();
+                    wmu[ring_m1] = mu.y();
+                    wM[ring_m0] = M.x();
+                    wM[ring_m1] = M.y();
                 }
                 // the plane barrier also tells every thread whether any wait ran out
                 if (__syncthreads_or(late)) { dead = true; return false; }
@@ -528,12 +560,13 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                         const int o0 = ob + j0 * BX, o1 = ob + j1 * BX;
                         const V2<T> mu = Qr.mu[i], M = Qr.M[i], c = Qr.c[i];
                         // y neighbours: pair i-1 / i+1, or a shared row at the column ends
-                        const V2<T> muym = i > 0 ? Qr.mu[i - 1] : V2<T>(nmu[o0 - BX], Qr.mu[H - 1].x());
-                        const V2<T> Mym = i > 0 ? Qr.M[i - 1] : V2<T>(nM[o0 - BX], Qr.M[H - 1].x());
-                        const V2<T> muyp = i < H - 1 ? Qr.mu[i + 1] : V2<T>(Qr.mu[0].y(), nmu[o1 + BX]);
-                        const V2<T> Myp = i < H - 1 ? Qr.M[i + 1] : V2<T>(Qr.M[0].y(), nM[o1 + BX]);
-                        const V2<T> muxp(nmu[o0 + 1], nmu[o1 + 1]), muxm(nmu[o0 - 1], nmu[o1 - 1]);
-                        const V2<T> Mxp(nM[o0 + 1], nM[o1 + 1]), Mxm(nM[o0 - 1], nM[o1 - 1]);
+                        const V2<T> muym = i > 0 ? Qr.mu[i - 1] : V2<T>(nmu[m_above], Qr.mu[H - 1].x());
+                        const V2<T> Mym = i > 0 ? Qr.M[i - 1] : V2<T>(nM[m_above], Qr.M[H - 1].x());
+                        const V2<T> muyp = i < H - 1 ? Qr.mu[i + 1] : V2<T>(Qr.mu[0].y(), nmu[m_below]);
+                        const V2<T> Myp = i < H - 1 ? Qr.M[i + 1] : V2<T>(Qr.M[0].y(), nM[m_below]);
+                        const int po = pofs + 2 * BX * i;              // the pair in the mu/M plane
+                        const V2<T> muxp = ld2(nmu + po + 2), muxm = ld2(nmu + po - 2);
+                        const V2<T> Mxp = ld2(nM + po + 2), Mxm = ld2(nM + po - 2);
                         // dc: the flux form of phasefield.c:374-384, tmp3 inside M'.
                         // The six face fluxes are summed first and added to c once,
                         // so c is rounded once per step.

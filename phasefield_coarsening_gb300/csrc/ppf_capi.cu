@@ -441,7 +441,9 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     if (!c) return seterr(PPF_EINVAL, "null context");
     if (!c->uploaded) return seterr(PPF_ESTATE, "autotuning needs an uploaded state");
     if (trial_steps < 1) trial_steps = 1;
-    // candidates: the model's chunk, powers of two, a single chunk; both unrolls
+    // candidates: the model's chunk, powers of two, a single chunk, and the
+    // chunks that deal k = 3..7 items to nearly every CTA (so that the
+    // resident CTAs end together); both unrolls
     int zcs[16], nzc = 0;
     auto add = [&](int z) {
         if (z < 1 || z > c->nz) return;
@@ -454,6 +456,17 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     for (int z = 8; z <= 128; z *= 2) add(z);
     add((c->tune.zc + 1) / 2);
     add(c->tune.zc * 2);
+    {
+        int tx = 0, ty = 0;
+        if (c->prec == PPF_F32) step_tile<float>(&tx, &ty);
+        else step_tile<double>(&tx, &ty);
+        const int64_t ntiles = (int64_t)((c->nx + tx - 1) / tx) * ((c->ny + ty - 1) / ty);
+        const int64_t slots = grid_for(c, 1);          // a grid that every CTA slot holds
+        for (int k = 3; k <= 7 && ntiles > 0 && slots > 0; ++k) {
+            const int64_t nc = k * slots / ntiles;     // chunks per tile column
+            if (nc >= 1) add((int)((c->nz + nc - 1) / nc));
+        }
+    }
     // keep the state: the trials advance it, so save it and restore it after
     const int64_t steps0 = c->steps;
     int rc = do_unpack(c);

@@ -431,33 +431,38 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
 
         // producer (thread 0): walks the same items and planes as the consumers,
         // S-2 loads ahead
-        int p_item = blockIdx.x, p_pz = 0;
+        int p_item = blockIdx.x, p_pz = 0, p_xs = 0, p_ys = 0;
+        const CUtensorMap *p_mS = &mapS, *p_mL = &mapL, *p_mC = &mapC;
         Item p_it;
         auto p_set = [&]() {
             if (p_item < nitems) {
                 p_it = item_at<MULTI>(p_item, ntiles1, zc1, g1.nz, table, ndom);
                 p_pz = p_it.z0 - 1;
+                // the item's box corner: storage x of the box start (16-byte
+                // aligned) and storage y of interior row y0-1
+                const int ntx = MULTI ? table[p_it.dom].ntx : ntx1;
+                const int xoff = MULTI ? table[p_it.dom].g.xoff : g1.xoff;
+                const int by = p_it.tile / ntx, bx = p_it.tile - by * ntx;
+                p_xs = bx * TX + xoff - XH;
+                p_ys = by * TY;
+                if (MULTI) {
+                    p_mS = &table[p_it.dom].maps[parity][0];
+                    p_mL = &table[p_it.dom].maps[parity][1];
+                    p_mC = &table[p_it.dom].maps[parity][2];
+                }
             }
         };
         p_set();
         int ist = 0, issued = 0;
         auto issue = [&]() {
             const uint32_t bar = smem_u32(&sm.bar[ist]);
-            const int ntx = MULTI ? table[p_it.dom].ntx : ntx1;
-            const int xoff = MULTI ? table[p_it.dom].g.xoff : g1.xoff;
-            const CUtensorMap *mS = MULTI ? &table[p_it.dom].maps[parity][0] : &mapS;
-            const CUtensorMap *mL = MULTI ? &table[p_it.dom].maps[parity][1] : &mapL;
-            const CUtensorMap *mC = MULTI ? &table[p_it.dom].maps[parity][2] : &mapC;
-            const int bx = p_it.tile % ntx, by = p_it.tile / ntx;
-            const int xs = bx * TX + xoff - XH;       // storage x of the box start (16-byte aligned)
-            const int ys = by * TY;                    // storage y of interior y0-1
             const int zs = p_pz + 1;                   // storage z of the plane
             uint32_t bytes = 3u * (uint32_t)G::BOX_BYTES;
             if (inject_stall && issued == 1) bytes += 16u;   // test hook: this phase can never complete
             mbar_expect_tx(bar, bytes);
-            tma_load_3d(smem_u32(sm.raw[ist][0]), mS, xs, ys, zs, bar);
-            tma_load_3d(smem_u32(sm.raw[ist][1]), mL, xs, ys, zs, bar);
-            tma_load_3d(smem_u32(sm.raw[ist][2]), mC, xs, ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][0]), p_mS, p_xs, p_ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][1]), p_mL, p_xs, p_ys, zs, bar);
+            tma_load_3d(smem_u32(sm.raw[ist][2]), p_mC, p_xs, p_ys, zs, bar);
             if (++p_pz > p_it.z1) {
                 p_item += gridDim.x;
                 p_set();

@@ -137,31 +137,6 @@ __device__ __forceinline__ float fast_rcp<float>(float x) {
 template <>
 __device__ __forceinline__ double fast_rcp<double>(double x) { return __drcp_rn(x); }
 
-// pass A (phasefield.c:328-332) for one cell: mu and M' = tmp3 M.  With
-// EQ (AS == AL) the denominator AS+(AL-AS)hS is the constant AS and mu =
-// AS (c - cL0 + (cL0-cS0) hS).  Returns 1/(etaS^2+etaL^2) for reuse.
-template <typename T, bool EQ>
-__device__ __forceinline__ T pass_a(const Coef<T> &k, T eS, T eL, T c, T &mu, T &Mt) {
-    const T s2 = eS * eS;
-    const T rs = fast_rcp(s2 + eL * eL);
-    const T h = s2 * rs;
-    const T w = c - k.cL0 + k.dc0 * h;
-    if (EQ) mu = k.A * w;
-    else mu = k.AsAl * fast_rcp(k.AS + k.dA * h) * w;
-    Mt = k.Mt0 + k.Mt1 * h;
-    return rs;
-}
-
-// pass A for an owned cell plus the centre-only part of pass B: tmp1 dmu
-// of phasefield.c:351-359 through the identity
-//   fS - fL - mu (cS - cL) = (CS-CL) - mu ((cS0-cL0) + (1/AS-1/AL)/2 mu).
-template <typename T, bool EQ>
-__device__ __forceinline__ void pass_a_own(const Coef<T> &k, T eS, T eL, T c, T &mu, T &Mt, T &dmu) {
-    const T rs = pass_a<T, EQ>(k, eS, eL, c, mu, Mt);
-    const T D = EQ ? k.dC - mu * k.q1 : k.dC - mu * (k.q1 + k.q2 * mu);
-    dmu = k.dm2 * (eS * eL) * (rs * rs) * D;
-}
-
 // Two cells of one thread evaluated together.  For float this is the
 // packed f32x2 arithmetic of sm_100+ (one instruction per pair); for double
 // it is plain scalar code.  Each lane is rounded exactly as the scalar
@@ -272,7 +247,11 @@ CoefV<T> make_coefv(const Coef<T> &k) {
     return v;
 }
 
-// pass A + the centre part of pass B (see pass_a_own) for a pair of cells
+// pass A (phasefield.c:328-332) for a pair of cells: mu and M' = tmp3 M,
+// with EQ (AS == AL) the denominator AS+(AL-AS)hS is the constant AS and
+// mu = AS (c - cL0 + (cL0-cS0) hS); plus the centre-only part of pass B,
+// tmp1 dmu of :351-359, through the identity
+//   fS - fL - mu (cS - cL) = (CS-CL) - mu ((cS0-cL0) + (1/AS-1/AL)/2 mu).
 template <typename T, bool EQ>
 __device__ __forceinline__ void pass_a_own2(const CoefV<T> &kv, V2<T> eS, V2<T> eL, V2<T> c, V2<T> &mu, V2<T> &Mt,
                                             V2<T> &dmu) {

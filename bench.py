@@ -13,7 +13,9 @@ The state (2 x 3 x 67 MB) is larger than L2, so no flush is needed.
 
 e2e: the same metric through the C-ABI with host buffers: each step uploads
 the state from pinned host memory (ppf_upload), advances 100 steps,
-reduces and downloads the state (ppf_download).
+reduces and downloads the state (ppf_download).  Two contexts on two
+streams, one host thread each, take alternate steps, so that one's copies
+over the host link overlap the other's stepping; wall clock over all steps.
 
 --impl reference: the reference program itself (phasefield.c, serial build
 with OpenMP on its three passes, oracle/build_ref.py) on the host cores,
@@ -31,6 +33,7 @@ import statistics
 import subprocess
 import sys
 import tempfile
+import threading
 import time
 
 REPO = os.path.dirname(os.path.abspath(__file__))
@@ -287,27 +290,43 @@ def run_ours(args):
     total_ms = max_over_ranks(total_ms)
     value = job_glups(world, cells, INNER * args.steps, total_ms * 1e-3)
 
-    # e2e through the C-ABI with pinned host buffers
+    # e2e through the C-ABI with pinned host buffers.  Every bench step
+    # uploads its input from pinned host memory, steps, reduces and downloads
+    # its result.  Two contexts on two streams, each driven by its own host
+    # thread (the C-ABI's one-context-per-thread model; the calls release
+    # the GIL), take alternate bench steps, so that one context's host-link
+    # copies overlap the other's stepping.
+    sim2 = ppf.Simulation(shape, ppf.params_default(dt=DT), bc="periodic", precision="f32")
+    stream2 = torch.cuda.Stream()
+    sim2.set_stream(stream2.cuda_stream)
+    sim2.set_tune(tune["zc"], tune["roll"])
     host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (eS, eL, c)]
-    outh = [torch.empty(shape, dtype=torch.float64).pin_memory() for _ in range(3)]
+    outh = [[torch.empty(shape, dtype=torch.float64).pin_memory() for _ in range(3)] for _ in range(2)]
     ptr_in = [h.data_ptr() for h in host]
-    ptr_out = [h.data_ptr() for h in outh]
 
-    def e2e_step():
-        sim.upload_from(*ptr_in)
-        sim.step(INNER)
-        st = sim.reduce()
-        sim.download_into(*ptr_out)
-        return st
+    def e2e_worker(s, outp, n):
+        ptr_out = [h.data_ptr() for h in outp]
+        for _ in range(n):
+            s.upload_from(*ptr_in)
+            s.step(INNER)
+            s.reduce()
+            s.download_into(*ptr_out)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
+    def e2e_run(n):
+        ths = [threading.Thread(target=e2e_worker, args=(s, o, (n + 1 - i) // 2))
+               for i, (s, o) in enumerate(zip((sim, sim2), outh))]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+
+    e2e_run(max(2, args.warmup))
     torch.cuda.synchronize()
     w0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
+    e2e_run(args.steps)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - w0
+    sim2.close()
     e2e_s = max_over_ranks(e2e_s)
     e2e_value = job_glups(world, cells, INNER * args.steps, e2e_s)
 
@@ -331,7 +350,10 @@ def run_ours(args):
                          "kernel": "step_tma_kernel<float> (fused step, TMA-fed)", "algorithmic_bytes_per_launch": ALG_BYTES_F32 * cells,
                          "avg_launch_us": round(step_ms * 1e3, 2), "peak_source": src},
             "e2e": {"value": round(e2e_value, 3), "unit": "GLUPS", "h2d_bytes_per_step": 3 * cells * 8,
-                    "d2h_bytes_per_step": 3 * cells * 8 + 8 * 8},
+                    "d2h_bytes_per_step": 3 * cells * 8 + 8 * 8,
+                    "how": "ppf_upload (pinned float64 host arrays) + 100 ppf_step + ppf_reduce + ppf_download "
+                           "per bench step; two contexts on two streams, one host thread each, take alternate "
+                           "bench steps so that copies overlap stepping; wall clock over all steps"},
             "gpu_launches": args.steps * (INNER + 1 + 2),
             "clocks": clk,
             "final_stats": {k: stats[k] for k in ("mass", "solid", "free_energy", "nonfinite")},

@@ -418,6 +418,11 @@ class Ensemble:
     def __exit__(self, *exc):
         self.close()
 
+    @property
+    def handle(self):
+        """The ppf_ensemble* handle for direct C-ABI calls."""
+        return self._h
+
     def __len__(self):
         return len(self.shapes)
 

@@ -19,9 +19,10 @@
 //   * pass B + C for plane z-1 then read x/y neighbours from shared memory,
 //     and write the new state straight to HBM, including the face ghosts
 //     the boundary condition defines (so the next step reads ready ghosts).
-// Every mbarrier wait is bounded by a time limit: on expiry the CTA sets an
-// error word, drains its own outstanding copies (again bounded) and exits
-// uniformly; the host reports PPF_ETIMEOUT.
+// Every mbarrier wait is bounded by a time limit: on expiry the waiting
+// thread sets the error word, the plane barrier (__syncthreads_or) tells the
+// whole CTA, which drains its own outstanding copies (again bounded) and
+// exits uniformly; the host reports PPF_ETIMEOUT.
 #pragma once
 
 #include <cuda.h>

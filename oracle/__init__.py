@@ -1,9 +1,11 @@
 """ORACLE -- test infrastructure, not product code.
 
 ctypes access to the CPU restatement of the reference step
-(oracle/ppf_oracle.c, built into oracle/_build/libppf_oracle.so) and to the
-patched reference build recipe (oracle/build_ref.py).  Only tests/, the
-smoke check and bench.py's CPU baseline import this package.
+(oracle/ppf_oracle.c, built into oracle/_build/libppf_oracle.so), to the
+oracle's own HDF5 subset (oracle/hdf5_shim/h5ref.c, independent of the
+product's HDF5 code) and to the patched reference build recipe
+(oracle/build_ref.py).  Only tests/, the smoke check and bench.py's CPU
+baseline and reference arm import this package.
 """
 from __future__ import annotations
 
@@ -50,6 +52,16 @@ def lib():
                                                                ctypes.c_void_p, ctypes.c_int64]
         L.ppf_oracle_derive.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ppf_oracle_derive.restype = None
+        L.h5ref_write.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                  ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int64), ctypes.c_int,
+                                  ctypes.POINTER(ctypes.c_int64)]
+        L.h5ref_dims.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
+        L.h5ref_read.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64]
+        L.h5ref_list.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
+                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int64)]
+        L.h5ref_read_any.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64,
+                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int64)]
+        L.h5ref_error.restype = ctypes.c_char_p
         _lib = L
     return _lib
 
@@ -107,3 +119,71 @@ def particles(etaS, bc=0, threshold=0.5) -> dict:
     n = int(out[0])
     return {"count": n, "mean_radius": out[1] / n if n else 0.0, "solid_volume": out[2],
             "largest_volume": out[3], "interface_area": out[4], "volumes": np.sort(vols[:n])}
+
+
+# ------------------------------------------------ the oracle's HDF5 subset --
+
+class H5Error(RuntimeError):
+    pass
+
+
+def _h5check(rc):
+    if rc != 0:
+        raise H5Error(f"h5ref error {rc}: {lib().h5ref_error().decode(errors='replace')}")
+
+
+def h5_write(path, fields: dict, float32=False, chunk=None):
+    """Rank-3 datasets of one shape, float64 (or float32) little endian,
+    contiguous or chunked (full-size edge chunks)."""
+    names = list(fields)
+    arrs = [np.ascontiguousarray(fields[n], dtype=np.float64) for n in names]
+    shape = arrs[0].shape
+    if any(a.ndim != 3 or a.shape != shape for a in arrs):
+        raise ValueError("all datasets must be rank-3 and of one shape")
+    cn = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+    cp = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+    dims = (ctypes.c_int64 * 3)(*shape)
+    ch = (ctypes.c_int64 * 3)(*chunk) if chunk is not None else None
+    _h5check(lib().h5ref_write(str(path).encode(), len(names), cn, cp, dims, int(bool(float32)), ch))
+
+
+def h5_read(path, name) -> np.ndarray:
+    d = (ctypes.c_int64 * 3)()
+    _h5check(lib().h5ref_dims(str(path).encode(), name.encode(), d))
+    out = np.empty(tuple(d), np.float64)
+    _h5check(lib().h5ref_read(str(path).encode(), name.encode(), out.ctypes.data, out.size))
+    return out
+
+
+def h5_list(path):
+    """[(name, rank, dims)] of the objects in the root group."""
+    out = []
+    for i in range(1 << 16):
+        name = ctypes.create_string_buffer(256)
+        rank = ctypes.c_int(0)
+        dims = (ctypes.c_int64 * 3)()
+        rc = lib().h5ref_list(str(path).encode(), i, name, 256, ctypes.byref(rank), dims)
+        if rc == -3:
+            break
+        _h5check(rc)
+        out.append((name.value.decode(), rank.value, tuple(dims)))
+    return out
+
+
+def h5_read_any(path, name, capacity=1 << 20) -> np.ndarray:
+    """A rank 1-3 contiguous float dataset of any HDF5 file, as stored."""
+    out = np.empty(capacity, np.float64)
+    rank = ctypes.c_int(0)
+    dims = (ctypes.c_int64 * 3)()
+    _h5check(lib().h5ref_read_any(str(path).encode(), name.encode(), out.ctypes.data, capacity, ctypes.byref(rank),
+                                  dims))
+    shape = tuple(dims)[:rank.value]
+    return out[:int(np.prod(shape))].reshape(shape).copy()
+
+
+def write_fields(path, etaS, etaL, c, chunk=None):
+    h5_write(path, {"etaS": etaS, "etaL": etaL, "c": c}, chunk=chunk)
+
+
+def read_fields(path):
+    return tuple(h5_read(path, n) for n in ("/etaS", "/etaL", "/c"))

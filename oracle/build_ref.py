@@ -7,7 +7,9 @@ The reference fixes its configuration at compile time with unguarded
 installed.  So the recipe reads phasefield.c where it lies, applies a fixed
 list of one-line substitutions, writes the patched translation unit to
 oracle/_ref/ (git-ignored; nothing from the reference is committed) and
-compiles it with gcc against the <hdf5.h> stand-in in oracle/hdf5_shim/.
+compiles it with gcc against the <hdf5.h> stand-in in oracle/hdf5_shim/
+(over the oracle's own HDF5 code, h5ref.c: no product code is linked).
+The reference source is read from $PPF_REFERENCE_SRC when that is set.
 
 Substitutions (each must match exactly once, else the build fails):
   phasefield.c:13      USE_MPI 1 -> 0 (serial build: MPI is absent)
@@ -42,10 +44,11 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
-REF_SRC = "/root/reference/phasefield.c"
+# where the reference source lies; PPF_REFERENCE_SRC overrides it
+REF_SRC = os.environ.get("PPF_REFERENCE_SRC", "/root/reference/phasefield.c")
 OUT_DIR = os.path.join(HERE, "_ref")
-H5LITE = os.path.join(REPO, "phasefield_coarsening_gb300", "csrc", "h5lite.c")
 SHIM = os.path.join(HERE, "hdf5_shim")
+H5REF = os.path.join(SHIM, "h5ref.c")
 
 
 def _sub_once(src: str, old: str, new: str) -> str:
@@ -128,10 +131,11 @@ def build(nz: int, ny: int, nx: int, bc: int = 0, n_iter: int = 1, n_save: int =
                 f.write(text)
     elif not os.path.exists(csrc):
         raise FileNotFoundError("reference sources absent and no patched unit in oracle/_ref/")
-    if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(csrc), os.path.getmtime(H5LITE)):
+    deps = [csrc, H5REF, os.path.join(SHIM, "h5shim.c"), os.path.join(SHIM, "h5ref.h"), os.path.join(SHIM, "hdf5.h")]
+    if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(p) for p in deps):
         return exe
-    cmd = ["gcc", "-std=gnu99", "-O2", "-w", "-I", SHIM, "-I", os.path.join(REPO, "include"),
-           csrc, os.path.join(SHIM, "h5shim.c"), H5LITE, "-o", exe + ".tmp", "-lm"]
+    cmd = ["gcc", "-std=gnu99", "-O2", "-w", "-I", SHIM, csrc, os.path.join(SHIM, "h5shim.c"), H5REF,
+           "-o", exe + ".tmp", "-lm"]
     if omp:
         cmd.insert(3, "-fopenmp")
     r = subprocess.run(cmd, capture_output=True, text=True)

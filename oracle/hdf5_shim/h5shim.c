@@ -1,7 +1,8 @@
 /*
  * ORACLE -- test infrastructure.  Implementation of the <hdf5.h> stand-in
- * (see hdf5.h here) over the project's HDF5 subset.  Supports the rank-3,
- * float64, unit-stride hyperslab transfers of phasefield.c:996-1109.
+ * (see hdf5.h here) over the oracle's own HDF5 subset (h5ref.c, independent
+ * of the product's HDF5 code).  Supports the rank-3, float64, unit-stride
+ * hyperslab transfers of phasefield.c:996-1109.
  */
 #include "hdf5.h"
 
@@ -10,7 +11,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include "ppf_h5.h"
+#include "h5ref.h"
 
 enum { K_FREE = 0, K_FILE, K_DSET, K_SPACE };
 
@@ -89,8 +90,8 @@ herr_t H5Fclose(hid_t file)
         const char *names[MAXDS];
         const double *data[MAXDS];
         for (int i = 0; i < f->nds; ++i) { names[i] = f->dsname[i]; data[i] = f->dsdata[i]; }
-        if (ppf_h5_write3d(f->path, f->nds, names, data, f->dsdims[0], PPF_H5_F64, NULL) != 0) {
-            fprintf(stderr, "HDF5-DIAG (shim): H5Fclose: %s\n", ppf_h5_last_error());
+        if (h5ref_write(f->path, f->nds, names, data, f->dsdims[0], 0, NULL) != 0) {
+            fprintf(stderr, "HDF5-DIAG (shim): H5Fclose: %s\n", h5ref_error());
             rc = -1;
         }
     }
@@ -105,8 +106,8 @@ hid_t H5Dopen2(hid_t loc, const char *name, hid_t dapl)
     obj *f = get(loc, K_FILE, "H5Dopen2");
     if (!f) return -1;
     int64_t dims[3];
-    if (ppf_h5_dims(f->path, name, dims) != 0) {
-        fprintf(stderr, "HDF5-DIAG (shim): H5Dopen2: %s\n", ppf_h5_last_error());
+    if (h5ref_dims(f->path, name, dims) != 0) {
+        fprintf(stderr, "HDF5-DIAG (shim): H5Dopen2: %s\n", h5ref_error());
         return -1;
     }
     hid_t id = new_obj(K_DSET);
@@ -210,16 +211,15 @@ herr_t H5Dread(hid_t dset, hid_t memtype, hid_t memspace, hid_t filespace, hid_t
         if (ms->count[i] != fs->count[i]) return -1;
     obj *f = get(d->file, K_FILE, "H5Dread");
     if (!f) return -1;
-    int64_t dims[3];
     size_t n = (size_t)(d->dims[0] * d->dims[1] * d->dims[2]);
     double *tmp = (double *)malloc(n * sizeof(double));
     if (!tmp) return -1;
-    if (ppf_h5_read3d(f->path, d->name, dims, tmp, (int64_t)n) != 0) {
-        fprintf(stderr, "HDF5-DIAG (shim): H5Dread: %s\n", ppf_h5_last_error());
+    if (h5ref_read(f->path, d->name, tmp, (int64_t)n) != 0) {
+        fprintf(stderr, "HDF5-DIAG (shim): H5Dread: %s\n", h5ref_error());
         free(tmp);
         return -1;
     }
-    copy_box(tmp, dims, fs->start, (double *)buf, ms->sdims, ms->start, ms->count);
+    copy_box(tmp, d->dims, fs->start, (double *)buf, ms->sdims, ms->start, ms->count);
     free(tmp);
     return 0;
 }

@@ -5,8 +5,8 @@
  * (phasefield.c:996-1109): H5Fopen/H5Fcreate/H5Fclose, H5Dopen2/
  * H5Dcreate2/H5Dclose/H5Dget_space/H5Dread/H5Dwrite, H5Screate_simple/
  * H5Sselect_hyperslab/H5Sclose.  h5shim.c implements them on top of the
- * project's HDF5 subset (include/ppf_h5.h), so files read and written by
- * the reference build are real HDF5 files.
+ * oracle's own HDF5 subset (h5ref.h), so files read and written by the
+ * reference build are real HDF5 files and no product code is involved.
  *
  * Like libhdf5, identifiers are never reused: an operation on a closed
  * identifier fails (returns a negative value) and leaves the buffer alone.

@@ -3,7 +3,8 @@
 Outputs (all git-ignored, in-tree):
   phasefield_coarsening_gb300/_build/libppf_gb300.so   C-ABI (include/ppf.h, include/ppf_h5.h)
   phasefield_coarsening_gb300/_build/ppf               drop-in for the reference's `ppf`
-  oracle/_build/libppf_oracle.so                       CPU restatement (test infrastructure)
+  oracle/_build/libppf_oracle.so                       CPU restatement + the oracle's own HDF5
+                                                       subset (test infrastructure)
 
 sm_103a only: every .cu file is compiled with
   -gencode arch=compute_103a,code=sm_103a -lineinfo
@@ -84,9 +85,12 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict:
         if _stale(obj, [c] + hdrs):
             jobs.append(["gcc", "-std=c99", "-O2", "-fPIC", "-Wall", "-I", INCLUDE, "-c", c, "-o", obj])
     oracle_src = os.path.join(ORACLE, "ppf_oracle.c")
-    if _stale(ORACLE_LIB, [oracle_src, os.path.join(ORACLE, "ppf_oracle.h"), os.path.join(INCLUDE, "ppf.h")]):
-        jobs.append(["gcc", "-std=c99", "-O2", "-fopenmp", "-fPIC", "-shared", "-I", INCLUDE, oracle_src, "-o",
-                     ORACLE_LIB, "-lm"])
+    shim = os.path.join(ORACLE, "hdf5_shim")
+    h5ref = os.path.join(shim, "h5ref.c")
+    if _stale(ORACLE_LIB, [oracle_src, h5ref, os.path.join(shim, "h5ref.h"), os.path.join(ORACLE, "ppf_oracle.h"),
+                           os.path.join(INCLUDE, "ppf.h")]):
+        jobs.append(["gcc", "-std=c99", "-O2", "-fopenmp", "-fPIC", "-shared", "-I", INCLUDE, "-I", shim, oracle_src,
+                     h5ref, "-o", ORACLE_LIB, "-lm"])
     logs = []
     with cf.ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
         for out in ex.map(_run, jobs):

@@ -490,6 +490,7 @@ static int put_chunk(rd_t *r, const dset_t *d, uint64_t addr, const int64_t off[
     int rc = rd_at(r, addr, raw, (size_t)(n * d->esize));
     if (rc) { free(raw); return rc; }
     double *row = (double *)malloc((size_t)cd[2] * sizeof(double));
+    if (!row) { free(raw); return fail(PPF_H5_ENOMEM, "h5: out of memory"); }
     for (int64_t i = 0; i < cd[0] && off[0] + i < d->dims[0]; ++i)
         for (int64_t j = 0; j < cd[1] && off[1] + j < d->dims[1]; ++j) {
             int64_t nk = cd[2];
@@ -523,8 +524,15 @@ static int chunk_btree(rd_t *r, const dset_t *d, uint64_t node, double *out, int
         if (level > 0) { rc = chunk_btree(r, d, child, out, depth + 1); continue; }
         if (get_le(k + 4, 4) != 0) { rc = fail(PPF_H5_EFORMAT, "h5: filtered chunk unsupported"); break; }
         int64_t off[3];
-        for (int q = 0; q < 3; ++q) off[q] = (int64_t)get_le(k + 8 + 8 * q, 8);
-        if (off[0] >= d->dims[0] || off[1] >= d->dims[1] || off[2] >= d->dims[2]) continue;
+        int bad = 0;
+        for (int q = 0; q < 3; ++q) {
+            const uint64_t u = get_le(k + 8 + 8 * q, 8);
+            /* a chunk origin is a multiple of the chunk size inside the
+             * dataset; anything else would place the copy outside `out` */
+            if (u >= (uint64_t)d->dims[q] || u % (uint64_t)d->cdims[q] != 0) bad = 1;
+            off[q] = (int64_t)u;
+        }
+        if (bad) { rc = fail(PPF_H5_EFORMAT, "h5: chunk offset outside the dataset or off the chunk grid"); break; }
         rc = put_chunk(r, d, child, off, out);
     }
     free(b);

@@ -5,8 +5,9 @@ The reference (jijn/phasefield_coarsening) has no tests and ships no
 fixtures, so its own output on small seeded inputs is the pin: each case is
 built with oracle/build_ref.py (the reference source with only its
 compile-time grid/BC/step constants patched, see that file), fed an input
-written with the project's HDF5 writer, and its output file and its stderr
-convergence line are stored next to the input in one .npz.
+written with the oracle's HDF5 writer (oracle/hdf5_shim/h5ref.c), and its
+output file and its stderr convergence line are stored next to the input in
+one .npz.
 
 Run from the repository root (needs the reference sources):
     python tests/golden/make_golden.py [case names]
@@ -65,7 +66,7 @@ CASES = {
 
 def make_case(name, spec, work):
     shape, bc, n_iter, n_save, n_init, dt_expr, fix, seed = spec[:8]
-    from phasefield_coarsening_gb300 import write_fields, read_fields
+    from oracle import read_fields, write_fields      # the oracle's HDF5 subset: no product code
     rng = np.random.default_rng(seed)
     if len(spec) > 8 and spec[8] == "uniform":
         etaS, etaL, c = np.zeros(shape), np.ones(shape), np.full(shape, 0.95)

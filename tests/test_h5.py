@@ -130,3 +130,77 @@ def test_metadata_dataset_round_trip(tmp_path):
         assert np.array_equal(ppf.h5_read(p, "ppf_restart").ravel(), rec)
         for k, v in f.items():
             assert np.array_equal(ppf.h5_read(p, k), v)
+
+
+# ---- two independent implementations of the format: the product's and the oracle's ----
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("shape,chunk", [((7, 9, 11), None), ((7, 9, 11), (2, 3, 4)), ((20, 33, 70), (5, 6, 7)),
+                                         ((9, 9, 9), (1, 1, 1)), ((16, 16, 16), (8, 8, 8))])
+def test_product_and_oracle_hdf5_read_each_other(tmp_path, dtype, shape, chunk):
+    """Files written by the oracle's HDF5 code (oracle/hdf5_shim/h5ref.c,
+    written separately from the format specification) read bit-exact with
+    the product's reader and vice versa: contiguous, chunked with partial
+    edge chunks, multi-level chunk B-trees (9^3 chunks of 1), float32."""
+    import oracle
+    f = _fields(shape, 11)
+    po, pp = str(tmp_path / "o.h5"), str(tmp_path / "p.h5")
+    oracle.h5_write(po, f, float32=dtype == "f32", chunk=chunk)
+    ppf.h5_write(pp, f, dtype=dtype, chunk=chunk)
+    for k, v in f.items():
+        want = v.astype(np.float32).astype(np.float64) if dtype == "f32" else v
+        assert np.array_equal(ppf.h5_read(po, k), want), k
+        assert np.array_equal(oracle.h5_read(pp, k), want), k
+        assert np.array_equal(oracle.h5_read(po, k), want), k
+
+
+def test_oracle_reader_reads_data_written_by_libhdf5():
+    """The MATLAB v7.3 fixture was written by libhdf5 (user block, base
+    address 512, layout message version 2): the oracle's reader finds the
+    rank-2 dataset and reads its values, x = 0:pi/4:2*pi."""
+    import oracle
+    p = _libhdf5_file()
+    if p is None:
+        pytest.skip("scipy test data not installed")
+    assert oracle.h5_list(p)[0][:2] == ("testdouble", 2)
+    x = oracle.h5_read_any(p, "testdouble")
+    assert x.shape == (9, 1)
+    assert np.allclose(x.ravel(), np.arange(9) * np.pi / 4, rtol=1e-15, atol=1e-15)
+
+
+def test_reference_side_links_no_product_code():
+    """The reference build's <hdf5.h> stand-in and the build recipe use the
+    oracle's HDF5 code only."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    shim = os.path.join(os.path.dirname(here), "oracle", "hdf5_shim")
+    for fn in ("h5shim.c", "h5ref.c", "h5ref.h", "hdf5.h"):
+        text = open(os.path.join(shim, fn)).read()
+        assert "ppf_h5" not in text and "h5lite" not in text, fn
+    recipe = open(os.path.join(os.path.dirname(here), "oracle", "build_ref.py")).read()
+    assert "h5lite" not in recipe and "phasefield_coarsening_gb300" not in recipe
+
+
+def _chunk_key_offsets(raw):
+    """Offsets of the first chunk key's z origin in each raw-data B-tree node."""
+    out, i = [], raw.find(b"TREE")
+    while i >= 0:
+        if raw[i + 4] == 1:
+            out.append(i + 24 + 8)
+        i = raw.find(b"TREE", i + 1)
+    return out
+
+
+@pytest.mark.parametrize("origin", [2 ** 63 + 4, 1, 2 ** 40])
+def test_malformed_chunk_origin_is_rejected(tmp_path, origin):
+    """A chunk origin outside the dataset or off the chunk grid is a format
+    error, never a copy outside the output array."""
+    p = str(tmp_path / "c.h5")
+    ppf.h5_write(p, _fields((6, 6, 6), 3), chunk=(2, 3, 3))
+    raw = bytearray(open(p, "rb").read())
+    at = _chunk_key_offsets(bytes(raw))[0]
+    raw[at:at + 8] = int(origin).to_bytes(8, "little")
+    bad = tmp_path / "bad.h5"
+    bad.write_bytes(bytes(raw))
+    with pytest.raises(ppf.PPFError) as e:
+        ppf.h5_read(str(bad), "etaS")
+    assert e.value.code == -2

@@ -58,7 +58,7 @@ def test_oracle_conserves_solute_periodic_and_noflux():
 @pytest.mark.parametrize("bc", [0, 1])
 def test_oracle_matches_fresh_reference_build(bc, tmp_path):
     br = build_ref
-    from phasefield_coarsening_gb300 import read_fields, write_fields
+    from oracle import read_fields, write_fields
     shape = (7, 9, 11)
     st = smooth_state(shape, seed=11 + bc)
     inp = str(tmp_path / "x.h5")

@@ -19,8 +19,16 @@ over the host link overlap the other's stepping; wall clock over all steps.
 
 --impl reference: the reference program itself (phasefield.c, serial build
 with OpenMP on its three passes, oracle/build_ref.py) on the host cores,
-same workload; each step is one run of 10 time steps timed by the
-program's own loop timer.
+same workload; each step is one run of 100 time steps (one bench step of
+this arm) timed by the program's own loop timer.  Its input file is written
+by the oracle's HDF5 code: the product library is never loaded there.
+
+Extra sections of the default line: fp64 (the FP64 fused step, the
+reference's precision, with its roofline against the measured FP64 FMA
+rate), surrogate (the learned K-step network with the stencil corrector),
+ensemble (64 domains in one persistent launch per time step).
+--workload ensemble64 and --workload coarsen512 (512^3, R-bar(t) every 1000
+steps for --steps x 1000 steps) print their own lines.
 
 Multi-GPU: replicas only (one independent domain per rank), max over ranks.
 """
@@ -360,20 +368,103 @@ def run_ours(args):
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample((eS, eL, c), cells)
+        if not args.no_fp64:
+            # the reference's precision on the GPU (the CPU arm computes in FP64)
+            line["fp64"] = fp64_section((eS, eL, c), shape)
         if not args.no_surrogate:
             line["surrogate"] = surrogate_section((eS, eL, c), shape)
+        if not args.no_ensemble:
+            line["ensemble"] = ensemble_section(args.seed, steps=max(3, args.steps // 4), warmup=2)
         print(json.dumps(line), flush=True)
     sim.close()
     if world > 1:
         dist.destroy_process_group()
 
 
+def ensemble_measure(doms, steps, warmup, world=1):
+    """The ensemble of domains `doms` advanced by one persistent launch per
+    time step under CUDA-graph replay, against the same domains stepped one
+    context at a time (64 launches per time step).  Host wall-clock around
+    step(n) + sync, so launch overheads count.  Returns (ensemble, section
+    dict, tune); the caller closes the ensemble."""
+    import numpy as np
+
+    import phasefield_coarsening_gb300 as ppf
+
+    shapes = [d[0].shape for d in doms]
+    cells = int(sum(np.prod(s) for s in shapes))
+    prm = ppf.params_default(dt=DT)
+    ens = ppf.Ensemble(shapes, prm, bc="periodic", precision="f32")
+    for i, (eS, eL, c, _) in enumerate(doms):
+        ens.upload(i, eS, eL, c)
+    tune = ens.autotune(trial_steps=5)
+
+    def timed(step_fn, sync_fn):
+        for _ in range(warmup):
+            step_fn()
+        sync_fn()
+        t = []
+        for _ in range(steps):
+            w0 = time.perf_counter()
+            step_fn()
+            sync_fn()
+            t.append(time.perf_counter() - w0)
+        return sum(t), t
+
+    ens_s, per = timed(lambda: ens.step(INNER), ens.sync)
+    ens_s = max_over_ranks(ens_s)
+    value = job_glups(world, cells, INNER * steps, ens_s)
+
+    sims = []
+    for eS, eL, c, _ in doms:
+        s = ppf.Simulation(eS.shape, prm, bc="periodic", precision="f32")
+        s.upload(eS, eL, c)
+        s.set_tune(tune["zc"], tune["roll"])
+        sims.append(s)
+
+    def seq_step():
+        for s in sims:
+            s.step(INNER)
+
+    seq_s, _ = timed(seq_step, lambda: [s.sync() for s in sims])
+    seq_s = max_over_ranks(seq_s)
+    seq_value = job_glups(world, cells, INNER * steps, seq_s)
+    # bit-exact agreement of the two paths on one domain after equal step counts
+    same = all(np.array_equal(a, b) for a, b in zip(ens.download(0), sims[0].download()))
+    for s in sims:
+        s.close()
+    hbm, src = peaks()
+    achieved = ALG_BYTES_F32 * cells * INNER * steps / ens_s / 1e9
+    sec = {
+        "workload": "ensemble64_edges48to128_vf10to40", "value": round(value, 3), "unit": "GLUPS",
+        "steps": steps, "warmup": warmup, "ms_per_step": round(1e3 * ens_s / steps, 4),
+        "spread": round((max(per) - min(per)) / min(per), 4) if per else None,
+        "domains": len(doms), "edges": sorted({s[0] for s in shapes}), "cells": cells,
+        "time_steps_per_bench_step": INNER, "launch": tune,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "peak_source": src,
+                     "what": "24 B per cell-step over all domains / host wall-clock of step(100) + sync"},
+        "sequential_contexts": {"value": round(seq_value, 3), "unit": "GLUPS",
+                                "how": "one ppf_step per domain per bench step, same launch choice"},
+        "sequential_equals_ensemble": bool(same),
+    }
+    return ens, sec, tune
+
+
+def ensemble_section(seed, steps, warmup):
+    """Config 2 as a section of the default line: 64 domains, K bench steps."""
+    from phasefield_coarsening_gb300 import ic
+    doms = ic.ensemble_workload(seed=seed)
+    ens, sec, _ = ensemble_measure(doms, steps, warmup)
+    ens.close()
+    return sec
+
+
 def run_ensemble(args):
     """--workload ensemble64: 64 periodic cubes (edges 48/64/96/128, solid
     fraction U[0.1, 0.4]) advanced by one persistent launch per time step
-    under CUDA-graph replay, against the same domains stepped one context at
-    a time (64 launches per time step).  Host wall-clock around
-    step(n) + sync, so launch overheads count."""
+    under CUDA-graph replay (see ensemble_measure), plus the end-to-end line
+    through the C-ABI with host buffers."""
     import numpy as np
     import torch
 
@@ -389,46 +480,10 @@ def run_ensemble(args):
     shapes = [d[0].shape for d in doms]
     cells = int(sum(np.prod(s) for s in shapes))
     prm = ppf.params_default(dt=DT)
-    ens = ppf.Ensemble(shapes, prm, bc="periodic", precision="f32")
-    for i, (eS, eL, c, _) in enumerate(doms):
-        ens.upload(i, eS, eL, c)
-    tune = ens.autotune(trial_steps=5)
-
-    def timed(step_fn, sync_fn):
-        for _ in range(args.warmup):
-            step_fn()
-        sync_fn()
-        t = []
-        for _ in range(args.steps):
-            w0 = time.perf_counter()
-            step_fn()
-            sync_fn()
-            t.append(time.perf_counter() - w0)
-        return sum(t)
-
     clocks = ClockSampler(local)
     clocks.start()
-    ens_s = max_over_ranks(timed(lambda: ens.step(INNER), ens.sync))
+    ens, sec, tune = ensemble_measure(doms, args.steps, args.warmup, world)
     clk = clocks.stop()
-    value = job_glups(world, cells, INNER * args.steps, ens_s)
-
-    sims = []
-    for eS, eL, c, _ in doms:
-        s = ppf.Simulation(eS.shape, prm, bc="periodic", precision="f32")
-        s.upload(eS, eL, c)
-        s.set_tune(tune["zc"], tune["roll"])
-        sims.append(s)
-
-    def seq_step():
-        for s in sims:
-            s.step(INNER)
-
-    seq_s = max_over_ranks(timed(seq_step, lambda: [s.sync() for s in sims]))
-    seq_value = job_glups(world, cells, INNER * args.steps, seq_s)
-    # bit-exact agreement of the two paths on one domain after equal step counts
-    same = all(np.array_equal(a, b) for a, b in zip(ens.download(0), sims[0].download()))
-    for s in sims:
-        s.close()
 
     # e2e through the C-ABI: every bench step uploads all domains from pinned
     # host memory, steps, and downloads all domains.  Two ensembles, one host
@@ -466,18 +521,17 @@ def run_ensemble(args):
     e2e_value = job_glups(world, cells, INNER * args.steps, e2e_s)
     if rank == 0:
         line = {
-            "metric": "GLUPS (ensemble of 64 domains, one persistent launch per time step)", "value": round(value, 3),
+            "metric": "GLUPS (ensemble of 64 domains, one persistent launch per time step)", "value": sec["value"],
             "unit": "GLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(1e3 * ens_s / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": sec["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": f"synthetic: {len(doms)} seeded sphere microstructures, {cells} cells in total",
-            "config": {"workload": "ensemble64_edges48to128_vf10to40", "domains": len(doms),
-                       "edges": sorted({s[0] for s in shapes}), "cells": cells, "bc": "periodic", "dt": DT,
-                       "time_steps_per_bench_step": INNER, "launch": tune,
+            "config": {"workload": sec["workload"], "domains": len(doms), "edges": sec["edges"], "cells": cells,
+                       "bc": "periodic", "dt": DT, "time_steps_per_bench_step": INNER, "launch": tune,
                        "l2": f"state {cells * 24 / 1e9:.2f} GB > 129 MB L2 (no flush needed)"},
-            "sequential_contexts": {"value": round(seq_value, 3), "unit": "GLUPS",
-                                    "how": "one ppf_step per domain per bench step, same launch choice"},
-            "sequential_equals_ensemble": bool(same),
+            "roofline": sec["roofline"],
+            "sequential_contexts": sec["sequential_contexts"],
+            "sequential_equals_ensemble": sec["sequential_equals_ensemble"],
             "e2e": {"value": round(e2e_value, 3), "unit": "GLUPS", "h2d_bytes_per_step": 3 * cells * 8,
                     "d2h_bytes_per_step": 3 * cells * 8,
                     "how": "ppf_ensemble_upload of every domain (pinned float64 host arrays) + 100 steps + "
@@ -490,6 +544,93 @@ def run_ensemble(args):
     ens.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+# FP64 arithmetic of one cell-step of the fused kernel with AS == AL (the
+# reference's constants): pass A 18 (incl. one reciprocal), pass B 61;
+# an FMA counts 2.  Algorithmic: the ring and halo-plane recomputation are
+# not counted.
+FP64_FLOP_PER_CELL = 79
+
+
+def fp64_section(state, shape, steps=30):
+    """The reference's precision on the GPU: the FP64 fused step on the same
+    256^3 state, device-timed (CUDA events on its stream), with its roofline
+    against this GPU's measured FP64 FMA rate (the FP64 pipe bounds it) and
+    its HBM fraction (48 B per cell-step)."""
+    import torch
+
+    import phasefield_coarsening_gb300 as ppf
+    cells = int(shape[0] * shape[1] * shape[2])
+    peak = ppf.measure_fp64_peak()
+    sim = ppf.Simulation(shape, ppf.params_default(dt=DT), bc="periodic", precision="f64")
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.upload(*state)
+    tune = sim.autotune(trial_steps=3)
+    sim.step(3)
+    sim.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.step(steps)
+    e1.record(stream)
+    sim.sync()
+    us = e0.elapsed_time(e1) * 1e3 / steps
+    sim.close()
+    tf = FP64_FLOP_PER_CELL * cells / (us * 1e-6) / 1e12
+    hbm, src = peaks()
+    gbs = 48 * cells / (us * 1e-6) / 1e9
+    return {
+        "kernel": "step_tma_kernel<double> (fused step, TMA-fed)", "value": round(cells / (us * 1e-6) / 1e9, 3),
+        "unit": "GLUPS", "us_per_step": round(us, 1), "steps": steps, "launch": tune,
+        "roofline": {"bound": "fp64", "achieved": round(tf, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
+                     "frac": round(tf / peak, 4), "flop_per_cell": FP64_FLOP_PER_CELL,
+                     "peak_source": "measured: ppf_measure_fp64_peak (DFMA chains on every SM, CUDA events)",
+                     "hbm_frac": round(gbs / hbm, 4), "hbm_achieved_gbs": round(gbs, 1)},
+    }
+
+
+def run_coarsen(args):
+    """--workload coarsen512: the long FP32 coarsening run (512^3 periodic,
+    solid fraction 0.2, lognormal radii of median 4, dt = 0.8 of the limit),
+    R-bar and the particle count every 1000 steps, the R-bar^3 ~ t fit.
+    --steps is the number of 1000-step observation intervals (default 100:
+    the configuration's 100k steps)."""
+    import torch
+
+    from phasefield_coarsening_gb300 import coarsen
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return
+    clocks = ClockSampler(local)
+    clocks.start()
+    r = coarsen.run("spheres512_lognormal4_vf20", steps=1000 * args.steps, every=1000, seed=args.seed)
+    clk = clocks.stop()
+    cells = 512 ** 3
+    line = {
+        "metric": "GLUPS (512^3 coarsening run, R-bar and count every 1000 steps)",
+        "value": round(r["glups_stepping"], 3), "unit": "GLUPS", "n_gpus": 1, "steps": args.steps, "warmup": 0,
+        "ms_per_step": round(1e3 * r["stepping_s"] / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": f"synthetic: {r['particles_initial']} seeded lognormal spheres (median R 4) at solid fraction 0.2",
+        "config": {"workload": "spheres512_lognormal4_vf20", "grid": r["grid"], "bc": "periodic", "dt": r["dt"],
+                   "time_steps_per_bench_step": 1000, "launch": r["launch"],
+                   "l2": f"state {cells * 24 / 1e9:.2f} GB > 129 MB L2 (no flush needed)"},
+        "wall_s": round(r["wall_s"], 2), "mass_drift_max": r["mass_drift_max"],
+        "free_energy_rel_change": r["free_energy_rel_change"], "fit": r["fit"],
+        "series": [{k: p[k] for k in ("step", "rbar", "count", "solid_fraction", "free_energy")} for p in r["series"]],
+        "gpu_launches": None, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _product_library_loaded() -> bool:
+    try:
+        with open("/proc/self/maps") as f:
+            return any("libppf_gb300" in ln for ln in f)
+    except OSError:
+        return False
 
 
 def run_reference(args):
@@ -555,6 +696,8 @@ def run_reference(args):
                          "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
+        # this process's mapped libraries: the product library must not be among them
+        "product_library_loaded": _product_library_loaded(),
     }
     print(json.dumps(line), flush=True)
 
@@ -570,7 +713,9 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--launch", type=int, nargs=2, metavar=("ZC", "ROLL"),
                     help="fixed launch choice of the stencil (z chunk, unroll 1 or 3) instead of autotuning")
-    ap.add_argument("--workload", choices=[WORKLOAD, "ensemble64"], default=WORKLOAD)
+    ap.add_argument("--workload", choices=[WORKLOAD, "ensemble64", "coarsen512"], default=WORKLOAD)
+    ap.add_argument("--no-ensemble", action="store_true", help="leave the ensemble section out of the default line")
+    ap.add_argument("--no-fp64", action="store_true", help="leave the FP64 section out of the default line")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("note: warm-up below 3 steps", file=sys.stderr)
@@ -578,6 +723,8 @@ def main():
         run_reference(args)
     elif args.workload == "ensemble64":
         run_ensemble(args)
+    elif args.workload == "coarsen512":
+        run_coarsen(args)
     else:
         run_ours(args)
 

@@ -214,7 +214,8 @@ int ppf_autotune(ppf_ctx *ctx, int trial_steps, ppf_tune *best);
  * allocated: the partial sums go to a fixed device array of the library,
  * which limits a call to PPF_NOALLOC_MAX_CELLS cells (larger grids get
  * PPF_EINVAL with a message).  The first call on a device looks up that
- * array's device address (do it before any stream capture).  Every call
+ * array's device address (do it before any stream capture), as does the
+ * first call after the device was reset.  Every call
  * shares the array: calls that overlap on the GPU race, so issue them on
  * one stream. */
 #define PPF_NOALLOC_MAX_CELLS 134217728   /* 512^3 */
@@ -246,6 +247,32 @@ int ppf_ensemble_get_tune(const ppf_ensemble *ens, ppf_tune *out);
 int ppf_ensemble_set_tune(ppf_ensemble *ens, const ppf_tune *t);
 /* Like ppf_autotune, over the whole ensemble (states kept). */
 int ppf_ensemble_autotune(ppf_ensemble *ens, int trial_steps, ppf_tune *best);
+
+/* Slabs: one domain split into z slabs, one context each, with one
+ * ghost-plane exchange per step -- the domain decomposition of the
+ * reference's MPI build (init_mpi, phasefield.c:627-679; the halo exchange
+ * exchange_ghost_layer, :683-708) along z.  After each step every slab's two
+ * z ghost planes are overwritten with its neighbours' boundary planes (the
+ * first and last slabs' outer planes wrap for PPF_BC_PERIODIC and keep
+ * their own mirror for PPF_BC_NOFLUX), so the result equals stepping the
+ * undivided domain bit for bit.  All slabs live on the current device. */
+typedef struct ppf_slabs ppf_slabs;
+
+/* The partition (no device needed): slab s holds planes [z0[s], z0[s] +
+ * nzs[s]); lower[s] / upper[s] is the slab whose boundary plane fills its
+ * lower / upper ghost plane, or -1 where the BC fills it.  Arrays hold
+ * nslabs entries; 1 <= nslabs <= nz. */
+int ppf_slabs_plan(int nz, int nslabs, int bc, int *z0, int *nzs, int *lower, int *upper);
+int ppf_slabs_create(int nz, int ny, int nx, int nslabs, const ppf_params *p, int bc, int precision,
+                     ppf_slabs **out);
+int ppf_slabs_destroy(ppf_slabs *s);
+/* Whole-domain host arrays, nz*ny*nx doubles in C order [z][y][x]. */
+int ppf_slabs_upload(ppf_slabs *s, const double *etaS, const double *etaL, const double *c);
+int ppf_slabs_download(ppf_slabs *s, double *etaS, double *etaL, double *c);
+int ppf_slabs_step(ppf_slabs *s, int64_t nsteps);
+/* Sums over the slabs of ppf_reduce's fields (steps: the slabs' count). */
+int ppf_slabs_reduce(ppf_slabs *s, ppf_stats *out);
+int ppf_slabs_sync(ppf_slabs *s);
 
 /* Solute-mass projection of an FP32 state: sum(c) over the interior is set
  * to target_mass (FP64 arithmetic; the deficit is spread over the cells in
@@ -305,6 +332,11 @@ int ppf_surrogate_advance(ppf_surrogate *s, ppf_ctx *ctx, int ncalls);
  * bounded wait runs out (ppf_set_wait_limit of the context it runs on) and
  * the context's next synchronising call returns PPF_ETIMEOUT. */
 int ppf_surrogate_debug_inject(ppf_surrogate *s, int fault);
+
+/* Measured FP64 FMA rate of the current device in TFLOP/s (2 FLOPs per
+ * FMA): the denominator of the FP64 step's roofline, which the FP64 pipe
+ * bounds on this GPU.  No counterpart in the reference.  Takes ~0.1 s. */
+int ppf_measure_fp64_peak(double *tflops);
 
 /* Message for the calling thread's last failure ("" if none). */
 const char *ppf_last_error(void);

@@ -31,11 +31,12 @@ EXPORTS = (
     "ppf_autotune", "ppf_observe_noalloc", "ppf_particles", "ppf_ensemble_create", "ppf_ensemble_destroy",
     "ppf_ensemble_domain", "ppf_ensemble_upload", "ppf_ensemble_download", "ppf_ensemble_step",
     "ppf_ensemble_reduce", "ppf_ensemble_sync", "ppf_ensemble_get_tune", "ppf_ensemble_set_tune",
-    "ppf_ensemble_autotune", "ppf_mass_project", "ppf_copy_state", "ppf_surrogate_config_default",
+    "ppf_ensemble_autotune", "ppf_slabs_plan", "ppf_slabs_create", "ppf_slabs_destroy", "ppf_slabs_upload",
+    "ppf_slabs_download", "ppf_slabs_step", "ppf_slabs_reduce", "ppf_slabs_sync", "ppf_mass_project", "ppf_copy_state", "ppf_surrogate_config_default",
     "ppf_surrogate_create", "ppf_surrogate_destroy", "ppf_surrogate_get_config", "ppf_surrogate_num_params",
     "ppf_surrogate_set_params", "ppf_surrogate_get_params", "ppf_surrogate_loss_grad", "ppf_surrogate_train_step",
-    "ppf_surrogate_predict", "ppf_surrogate_advance", "ppf_surrogate_debug_inject", "ppf_last_error",
-    "ppf_version",
+    "ppf_surrogate_predict", "ppf_surrogate_advance", "ppf_surrogate_debug_inject", "ppf_measure_fp64_peak",
+    "ppf_last_error", "ppf_version",
     "ppf_h5_dims", "ppf_h5_read3d", "ppf_h5_write3d", "ppf_h5_write3d_meta", "ppf_h5_last_error",
 )
 
@@ -146,6 +147,15 @@ def lib() -> ctypes.CDLL:
         L.ppf_ensemble_get_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
         L.ppf_ensemble_set_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
         L.ppf_ensemble_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Tune)]
+        L.ppf_slabs_plan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 4
+        L.ppf_slabs_create.argtypes = [ctypes.c_int] * 4 + [ctypes.POINTER(Params), ctypes.c_int, ctypes.c_int,
+                                                           ctypes.POINTER(ctypes.c_void_p)]
+        for n in ("ppf_slabs_destroy", "ppf_slabs_sync"):
+            getattr(L, n).argtypes = [ctypes.c_void_p]
+        for n in ("ppf_slabs_upload", "ppf_slabs_download"):
+            getattr(L, n).argtypes = [ctypes.c_void_p] * 4
+        L.ppf_slabs_step.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+        L.ppf_slabs_reduce.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
         L.ppf_mass_project.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.ppf_copy_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.ppf_surrogate_config_default.argtypes = [ctypes.POINTER(SurrogateConfig)]
@@ -164,6 +174,7 @@ def lib() -> ctypes.CDLL:
         L.ppf_surrogate_predict.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.ppf_surrogate_advance.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.ppf_surrogate_debug_inject.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ppf_measure_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
         L.ppf_h5_dims.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.ppf_h5_read3d.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _dp,
                                     ctypes.c_int64]
@@ -470,6 +481,69 @@ class Ensemble:
         return t.as_dict()
 
 
+def slabs_plan(nz: int, nslabs: int, bc="periodic") -> dict:
+    """ppf_slabs_plan: {z0, nz, lower, upper} lists (no device needed)."""
+    arrs = [(ctypes.c_int * nslabs)() for _ in range(4)]
+    _check(lib().ppf_slabs_plan(int(nz), int(nslabs), _BC[bc], *arrs))
+    return {k: list(a) for k, a in zip(("z0", "nz", "lower", "upper"), arrs)}
+
+
+class Slabs:
+    """Host-side mirror of a ppf_slabs: one domain as z slabs (one context
+    each) with a ghost-plane exchange per step."""
+
+    def __init__(self, shape, nslabs, params: Params | None = None, bc="periodic", precision="f64"):
+        nz, ny, nx = (int(v) for v in shape)
+        self.shape = (nz, ny, nx)
+        self.params = params if params is not None else params_default()
+        h = ctypes.c_void_p()
+        _check(lib().ppf_slabs_create(nz, ny, nx, int(nslabs), ctypes.byref(self.params), _BC[bc], _PREC[precision],
+                                      ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ppf_slabs_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload(self, etaS, etaL, c):
+        a = [_c64(x) for x in (etaS, etaL, c)]
+        if any(x.shape != self.shape for x in a):
+            raise ValueError("field shape does not match the domain")
+        _check(lib().ppf_slabs_upload(self._h, *[x.ctypes.data for x in a]))
+
+    def download(self):
+        out = [np.empty(self.shape, np.float64) for _ in range(3)]
+        _check(lib().ppf_slabs_download(self._h, *[x.ctypes.data for x in out]))
+        return tuple(out)
+
+    def step(self, n=1):
+        _check(lib().ppf_slabs_step(self._h, int(n)))
+
+    def sync(self):
+        _check(lib().ppf_slabs_sync(self._h))
+
+    def reduce(self) -> dict:
+        s = Stats()
+        _check(lib().ppf_slabs_reduce(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+
+def measure_fp64_peak() -> float:
+    """The current device's FP64 FMA rate, TFLOP/s (roofline of the FP64 step)."""
+    v = ctypes.c_double()
+    _check(lib().ppf_measure_fp64_peak(ctypes.byref(v)))
+    return v.value
+
+
 # ---------------------------------------------------------------- HDF5 ----
 
 def h5_dims(path: str, name: str):
@@ -520,6 +594,6 @@ def write_fields(path: str, etaS, etaL, c, dtype="f64", chunk=None):
     h5_write(path, {"etaS": etaS, "etaL": etaL, "c": c}, dtype=dtype, chunk=chunk)
 
 
-__all__ = ["Simulation", "Ensemble", "Params", "Stats", "Derived", "PPFError", "params_default", "derive", "lib",
+__all__ = ["Simulation", "Ensemble", "Slabs", "slabs_plan", "Params", "Stats", "Derived", "PPFError", "params_default", "derive", "lib",
            "h5_read", "h5_write", "h5_dims", "read_fields", "write_fields", "BC_PERIODIC", "BC_NOFLUX",
            "F64", "F32", "LIB_PATH", "EXE_PATH", "EXPORTS"]

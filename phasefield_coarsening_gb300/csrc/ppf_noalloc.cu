@@ -15,13 +15,18 @@
 // device address (it names a host-side stand-in); its device address is
 // looked up with cudaGetSymbolAddress once per device, the first time the
 // entry point runs with that device current.  That first call therefore
-// does set-up work and should come before any stream capture.
+// does set-up work and should come before any stream capture.  The address
+// is kept together with the identity of the CUDA context it belongs to: if
+// the caller resets the device (cudaDeviceReset), the next call finds a new
+// context and looks the address up again instead of using a stale one.
 //
 // The array is shared by every call in the process and keeps the last
 // call's contents.  Each call writes every partial slot it later reads, so
 // nothing in it has to start at zero.  Calls whose work overlaps on the GPU
 // (different streams, or different host threads) race on the array:
 // serialize them, e.g. by issuing them on one stream.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -147,10 +152,38 @@ __global__ void __launch_bounds__(kThreads) sum_partials(const double *__restric
     }
 }
 
-// device address of g_partials, looked up once per device
+// device address of g_partials, looked up once per device and context
 constexpr int kMaxDevices = 64;
-double *g_addr[kMaxDevices];
+struct ScratchAddr {
+    double *addr;
+    unsigned long long ctx_id;   // the CUDA context the address belongs to (unique per process)
+};
+ScratchAddr g_addr[kMaxDevices];
 std::mutex g_lock;
+
+// the unique id of the calling thread's current CUDA context (0: none yet)
+unsigned long long current_context_id() {
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (PFN_cuCtxGetCurrent_v4000)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (PFN_cuCtxGetId_v12000)p;
+        looked_up = true;
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 int scratch_for_current_device(double **out) {
     int dev = 0;
@@ -158,14 +191,19 @@ int scratch_for_current_device(double **out) {
     if (e != cudaSuccess) return fail(PPF_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return fail(PPF_ECUDA, "device %d out of range", dev);
     std::lock_guard<std::mutex> hold(g_lock);
-    if (!g_addr[dev]) {
+    ScratchAddr &a = g_addr[dev];
+    const unsigned long long id = current_context_id();
+    if (!a.addr || id == 0 || id != a.ctx_id) {
+        // first use on this device, or its context was recreated (cudaDeviceReset):
+        // the symbol's address belongs to the context's copy of this module
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_partials);
         if (e != cudaSuccess || !p)
             return fail(PPF_ECUDA, "cudaGetSymbolAddress of the reduction scratch: %s", cudaGetErrorString(e));
-        g_addr[dev] = static_cast<double *>(p);
+        a.addr = static_cast<double *>(p);
+        a.ctx_id = current_context_id();    // the lookup made the primary context current
     }
-    *out = g_addr[dev];
+    *out = a.addr;
     return PPF_OK;
 }
 

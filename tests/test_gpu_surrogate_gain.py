@@ -1,9 +1,10 @@
 """What the trained surrogate gains over the method without it: on an unseen
 microstructure, one call of the committed K = 50 network lands much closer
 to the stencil's state after 50 steps than leaving the state unchanged (the
-identity, i.e. surrogate + corrector with an untrained zero network) does;
-and the surrogate + corrector stepper keeps the solute mass on its initial
-value."""
+identity, i.e. surrogate + corrector with an untrained zero network) does,
+field by field; over many calls etaL and c stay far closer than the
+identity while etaS does not; and the surrogate + corrector stepper keeps
+the solute mass on its initial value."""
 import os
 
 import numpy as np
@@ -35,12 +36,36 @@ def test_trained_network_beats_the_identity():
     c = sim_of(shape, a.download())
     net.advance(c, 1)                            # the network's answer
     x, y, z = a.download(), b.download(), c.download()
-    e_id = sum(float(np.mean(((q - p) / sc) ** 2)) for p, q, sc in zip(x, y, scale))
-    e_net = sum(float(np.mean(((q - r) / sc) ** 2)) for q, r, sc in zip(y, z, scale))
+    e_id = [float(np.mean(((q - p) / sc) ** 2)) for p, q, sc in zip(x, y, scale)]
+    e_net = [float(np.mean(((q - r) / sc) ** 2)) for q, r, sc in zip(y, z, scale)]
     for s in (a, b, c):
         s.close()
     net.close()
-    assert e_net < 0.5 * e_id, (e_net, e_id)
+    # every field, one call: at least 2x closer than no change (normalised squared error)
+    for name, n, i in zip(("etaS", "etaL", "c"), e_net, e_id):
+        assert n < 0.5 * i, (name, n, i)
+
+
+def test_many_cycles_per_field_against_the_identity():
+    """Four stepper cycles (10 calls of K = 50 + 50 corrector steps each) on
+    an unseen microstructure, per field ||surrogate - stencil|| /
+    ||stencil - start|| against the same schedule with the calls replaced by
+    the identity.  etaL and c: the network carries most of the change.
+    etaS: the per-call errors accumulate (the network is trained on states
+    that change faster than these late, relaxed ones), and over many calls
+    the result is no better than leaving etaS unchanged; the bound records
+    that finding rather than hiding it."""
+    net = S.load(WEIGHTS)
+    shape = (32, 128, 128)
+    state = S.microstructure(shape, seed=515151, vf=0.25)
+    r = S.compare_to_stencil(net, state, cycles=4, calls=10, corrector_steps=50, warmup=500)
+    net.close()
+    f = r["field_err_vs_change"]
+    print(f)
+    assert f["surrogate"]["etaL"] < 0.6 * f["identity"]["etaL"]
+    assert f["surrogate"]["c"] < 0.6 * f["identity"]["c"]
+    assert f["surrogate"]["etaS"] < 2.0 * f["identity"]["etaS"]
+    assert r["mass_drift"] <= 1e-12 and r["fallbacks"] == 0
 
 
 def test_stepper_conserves_mass_and_counts_steps():

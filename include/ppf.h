@@ -187,6 +187,10 @@ typedef struct ppf_tune {
     int zc;              /* z planes per work item of the persistent grid */
     int roll;            /* 1: one plane body (the default), 3: unrolled three times */
     int grid;            /* CTAs (derived from zc; ignored by ppf_set_tune) */
+    int pdl;             /* 1 (the default): consecutive steps overlap by programmatic dependent
+                            launch (the next step's CTAs are placed while this one's last CTAs
+                            finish; every memory access still waits for the previous step);
+                            0: plain launches.  Ensembles ignore it. */
     double us_per_step;  /* measured time of the winner (ppf_autotune only) */
 } ppf_tune;
 

@@ -48,15 +48,20 @@ def fit_rbar3(series) -> dict:
            "rbar_rel_change": (series[-1]["rbar"] - series[0]["rbar"]) / series[0]["rbar"] if series[0]["rbar"] else 0.0,
            "count_first": series[0]["count"], "count_last": series[-1]["count"]}
     if len(series) >= 2 and np.ptp(t) > 0:
-        A = np.vstack([np.ones_like(t), t]).T
-        coef, *_ = np.linalg.lstsq(A, r3, rcond=None)
-        pred = A @ coef
-        ss_res = float(((r3 - pred) ** 2).sum())
-        ss_tot = float(((r3 - r3.mean()) ** 2).sum())
-        out.update({"k_rbar3_per_time": float(coef[1]), "rbar3_at_0": float(coef[0]),
-                    "r2": 1.0 - ss_res / ss_tot if ss_tot > 0 else None,
+        # centred and scaled coordinates: the times reach ~1e18 in the
+        # reference's units, far beyond what an unscaled solve resolves
+        tm, ts = t.mean(), np.ptp(t)
+        u = (t - tm) / ts
+        y = r3 - r3.mean()
+        k_u = float((u * y).sum() / (u * u).sum())
+        ss_res = float(((y - k_u * u) ** 2).sum())
+        ss_tot = float((y * y).sum())
+        k = k_u / ts
+        out.update({"k_rbar3_per_time": k, "rbar3_at_0": float(r3.mean() - k * tm),
+                    # no R^2 when R-bar^3 does not vary beyond round-off
+                    "r2": 1.0 - ss_res / ss_tot if ss_tot > 1e-24 * float((r3 * r3).sum()) else None,
                     # the same rate per explicit step, in cells^3
-                    "k_rbar3_per_step": float(coef[1]) * series[-1]["time"] / max(1, series[-1]["step"])})
+                    "k_rbar3_per_step": k * series[-1]["time"] / max(1, series[-1]["step"])})
     return out
 
 

@@ -24,6 +24,12 @@ using namespace ppf;
 
 static thread_local char g_err[512];
 
+// Consecutive steps overlap by programmatic dependent launch unless the
+// autotuner finds the plain launch faster: the next step's CTAs are placed
+// while this one's last CTAs drain (worth ~12 % per step at 128^3, nothing
+// at 256^3, where the step is long against the launch gap).
+static constexpr int kStepPdl = 1;
+
 static int seterr(int code, const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -191,6 +197,7 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
             }
         }
     c->tune.roll = 1;
+    c->tune.pdl = kStepPdl;
     c->tune.grid = precision == PPF_F32 ? tma_grid<float>(c->g, c->num_sms, &c->tune.zc)
                                         : tma_grid<double>(c->g, c->num_sms, &c->tune.zc);
     if (c->tune.grid < 1) {
@@ -420,6 +427,7 @@ extern "C" int ppf_get_tune(const ppf_ctx *c, ppf_tune *t) {
     t->zc = c->tune.zc;
     t->roll = c->tune.roll;
     t->grid = c->tune.grid;
+    t->pdl = c->tune.pdl;
     t->us_per_step = 0.0;
     return PPF_OK;
 }
@@ -428,12 +436,14 @@ extern "C" int ppf_set_tune(ppf_ctx *c, const ppf_tune *t) {
     if (!c || !t) return seterr(PPF_EINVAL, "null argument");
     if (t->roll != 1 && t->roll != 3) return seterr(PPF_EINVAL, "roll must be 1 or 3");
     if (t->zc < 1 || t->zc > c->nz) return seterr(PPF_EINVAL, "zc must be in [1, nz]");
+    if (t->pdl != 0 && t->pdl != 1) return seterr(PPF_EINVAL, "pdl must be 0 or 1");
     CU(cudaStreamSynchronize(c->stream));
     const int grid = grid_for(c, t->zc);
     if (grid < 1) return seterr(PPF_ECUDA, "no launch shape for zc=%d", t->zc);
     c->tune.zc = t->zc;
     c->tune.roll = t->roll;
     c->tune.grid = grid;
+    c->tune.pdl = t->pdl;
     return PPF_OK;
 }
 
@@ -443,7 +453,8 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     if (trial_steps < 1) trial_steps = 1;
     // candidates: the model's chunk, powers of two, a single chunk, and the
     // chunks that deal k = 3..7 items to nearly every CTA (so that the
-    // resident CTAs end together); both unrolls
+    // resident CTAs end together); both unrolls; with and without
+    // programmatic dependent launch
     int zcs[16], nzc = 0;
     auto add = [&](int z) {
         if (z < 1 || z > c->nz) return;
@@ -477,9 +488,11 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     CU(cudaEventCreate(&e1));
     float best_ms = -1.0f;
     StepTune win = keep;
+    for (int pdl = 1; pdl >= 0 && rc == PPF_OK; --pdl)
     for (int r = 0; r < 2 && rc == PPF_OK; ++r)
         for (int i = 0; i < nzc && rc == PPF_OK; ++i) {
-            StepTune t;
+            StepTune t = keep;
+            t.pdl = pdl;
             t.roll = r == 0 ? 3 : 1;
             t.zc = zcs[i];
             t.grid = grid_for(c, t.zc);
@@ -512,6 +525,7 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
         best->zc = win.zc;
         best->roll = win.roll;
         best->grid = win.grid;
+        best->pdl = win.pdl;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }
     return PPF_OK;

@@ -12,6 +12,7 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -61,6 +62,7 @@ __global__ void domain_sums(const DomainDesc *__restrict__ table, const double *
 struct ppf_ensemble {
     int n, prec, bc, eqA;
     std::vector<ppf_ctx *> dom;
+    std::vector<int> order;      // table entry k describes domain order[k]: largest domains first
     DomainDesc *dtable;          // device
     double **ddres;              // device: each domain's dres pointer
     double *partials;            // 3 doubles per work item
@@ -82,9 +84,9 @@ static int build_table(ppf_ensemble *e) {
     else step_tile<double>(&tx, &ty);
     std::vector<DomainDesc> h((size_t)e->n);
     int64_t item0 = 0;
-    for (int d = 0; d < e->n; ++d) {
-        ppf_ctx *c = e->dom[(size_t)d];
-        DomainDesc &t = h[(size_t)d];
+    for (int k = 0; k < e->n; ++k) {
+        ppf_ctx *c = e->dom[(size_t)e->order[(size_t)k]];
+        DomainDesc &t = h[(size_t)k];
         memset(&t, 0, sizeof t);
         for (int b = 0; b < 2; ++b)
             for (int f = 0; f < 3; ++f) {
@@ -198,11 +200,17 @@ extern "C" int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, 
         ppf_ensemble_destroy(e);
         return err_(PPF_ECUDA, "ensemble setup: %s", cudaGetErrorString(ce));
     }
+    // work items of the largest domains first: the persistent grid ends a
+    // step on the small domains' items, which shortens its tail
+    e->order.resize((size_t)n);
+    for (int d = 0; d < n; ++d) e->order[(size_t)d] = d;
+    std::stable_sort(e->order.begin(), e->order.end(), [&](int a, int b) {
+        const ppf_ctx *x = e->dom[(size_t)a], *y = e->dom[(size_t)b];
+        return (int64_t)x->nz * x->ny * x->nx > (int64_t)y->nz * y->ny * y->nx;
+    });
     std::vector<double *> h((size_t)n);
-    for (int d = 0; d < n; ++d) {
-        h[(size_t)d] = e->dom[(size_t)d]->dres;
-        e->dom[(size_t)d]->stream = e->stream;   // one stream orders every domain's work
-    }
+    for (int k = 0; k < n; ++k) h[(size_t)k] = e->dom[(size_t)e->order[(size_t)k]]->dres;
+    for (int d = 0; d < n; ++d) e->dom[(size_t)d]->stream = e->stream;   // one stream orders every domain's work
     ce = cudaMemcpy(e->ddres, h.data(), (size_t)n * sizeof(double *), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) {
         ppf_ensemble_destroy(e);
@@ -305,6 +313,7 @@ extern "C" int ppf_ensemble_get_tune(const ppf_ensemble *e, ppf_tune *t) {
     t->zc = e->zc;
     t->roll = e->roll;
     t->grid = e->grid;
+    t->pdl = 0;
     t->us_per_step = 0;
     return PPF_OK;
 }
@@ -372,6 +381,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
         best->zc = e->zc;
         best->roll = e->roll;
         best->grid = e->grid;
+        best->pdl = 0;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }
     return PPF_OK;

@@ -368,6 +368,13 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const uint32_t pad = (128u - (smem_u32(smem_dyn) & 127u)) & 127u;
     TmaSmem<T> &sm = *reinterpret_cast<TmaSmem<T> *>(smem_dyn + pad);
 
+    // programmatic dependent launch: let the next step's grid be scheduled
+    // now (its CTAs take SM slots as this grid's CTAs leave), and wait for
+    // the previous grid -- which reads what this one writes and writes what
+    // it reads -- to complete before touching global memory.  Both are no-ops
+    // when the launch does not allow the overlap.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = (warp % G::WX) * 32 + lane;        // own column in the tile
     const int ty0 = (warp / G::WX) * CY;              // first own row in the tile
@@ -870,19 +877,40 @@ int tma_grid_for_zc(const Geom &g, int num_sms, int zc) {
     return (int)(items < slots ? items : slots);
 }
 
+// A launch of the single-domain step; with `pdl` the launch allows
+// programmatic dependent launch (the kernel's griddepcontrol.wait keeps the
+// stream order for every global memory access).
+template <typename... KArgs, typename... Args>
+static void launch_step_ex(bool pdl, void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                           Args... args) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    (void)cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 template <typename T, int R, bool FULL>
 static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only, bool eqA,
-                     double *partials, int grid, int zc, int *err, unsigned long long limit_ns, int inject_stall,
+                     double *partials, const StepTune &tune, int *err, unsigned long long limit_ns, int inject_stall,
                      cudaStream_t s) {
     using G = TmaGeo<T>;
     const int ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
     const size_t sh = tma_smem_bytes<T>();
     const bool st = partials != nullptr;
     const CoefV<T> kv = make_coefv(k);
-#define PPF_LAUNCH(ST, CO, EQ)                                                                                   \
-    step_tma_kernel<T, ST, CO, EQ, R, false, FULL><<<grid, G::NT, sh, s>>>(                                     \
-        maps[0], maps[1], maps[2], g, k, kv, out, ntx, nty, zc, partials, err, limit_ns, inject_stall, nullptr, 0, \
-        0, 0)
+    const DomainDesc *no_table = nullptr;
+#define PPF_LAUNCH(ST, CO, EQ)                                                                                        \
+    launch_step_ex(tune.pdl != 0, step_tma_kernel<T, ST, CO, EQ, R, false, FULL>, tune.grid, G::NT, sh, s, maps[0],   \
+                   maps[1], maps[2], g, k, kv, out, ntx, nty, tune.zc, partials, err, limit_ns, inject_stall,        \
+                   no_table, 0, 0, 0)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -901,15 +929,11 @@ cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *
     // FULL: every tile inside the domain, and every element offset below 2^32
     const bool full = g.nx % G::TX == 0 && g.ny % G::TY == 0 && g.total <= ((int64_t)1 << 32);
     if (tune.roll == 1) {
-        if (full) launch_r<T, 1, true>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns,
-                                       inject_stall, s);
-        else launch_r<T, 1, false>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns,
-                                   inject_stall, s);
+        if (full) launch_r<T, 1, true>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, s);
+        else launch_r<T, 1, false>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, s);
     } else {
-        if (full) launch_r<T, 3, true>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns,
-                                       inject_stall, s);
-        else launch_r<T, 3, false>(g, k, maps, out, c_only, eqA, partials, tune.grid, tune.zc, err, limit_ns,
-                                   inject_stall, s);
+        if (full) launch_r<T, 3, true>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, s);
+        else launch_r<T, 3, false>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, s);
     }
     return cudaGetLastError();
 }

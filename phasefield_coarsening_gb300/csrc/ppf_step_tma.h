@@ -24,6 +24,7 @@ struct StepTune {
     int grid;   // persistent CTAs
     int zc;     // z planes per work item
     int roll;   // 3: plane body unrolled three times; 1: one copy
+    int pdl;    // 1: consecutive launches overlap by programmatic dependent launch
 };
 
 // Tensor map of one padded field (3-D: x pitch, ny+2 rows, nz+2 planes)

@@ -263,10 +263,10 @@ def test_launch_choices_are_bit_identical(precision):
     shape = (40, 35, 70)
     st = smooth_state(shape, seed=12)
     ref = None
-    for zc, roll in [(None, None), (1, 3), (7, 1), (40, 3), (13, 1)]:
+    for zc, roll, pdl in [(None, None, None), (1, 3, 1), (7, 1, 0), (40, 3, 0), (13, 1, 1)]:
         with ppf.Simulation(shape, bc=1, precision=precision) as s:
             if zc is not None:
-                s.set_tune(zc, roll)
+                s.set_tune(zc, roll, pdl)
             s.upload(*st)
             s.step(6)
             out = s.download()
@@ -274,7 +274,7 @@ def test_launch_choices_are_bit_identical(precision):
             ref = out
         else:
             for a, b in zip(out, ref):
-                assert np.array_equal(a, b), (zc, roll)
+                assert np.array_equal(a, b), (zc, roll, pdl)
 
 
 def test_autotune_keeps_state_and_picks_a_valid_choice():

@@ -29,7 +29,7 @@ def sim_of(shape, state):
 
 @pytest.mark.parametrize("weights", K50)
 def test_trained_network_beats_the_identity(weights):
-    net = S.load(os.path.join(WEIGHTS_DIR, weights))
+    net = S.load(os.path.join(WEIGHTS_DIR, weights), gain=(1.0, 1.0, 1.0))   # the raw network, one call
     k = net.config["k_steps"]
     scale = np.asarray(net.config["out_scale"])
     shape = (32, 128, 128)
@@ -58,10 +58,12 @@ def test_many_cycles_per_field_against_the_identity(weights):
     an unseen microstructure, per field ||surrogate - stencil|| /
     ||stencil - start|| against the same schedule with the calls replaced by
     the identity.  etaL and c: the network carries most of the change.
-    etaS: the per-call errors accumulate (the network is trained on states
-    that change faster than these late, relaxed ones), and over many calls
-    the result is no better than leaving etaS unchanged; the bound records
-    that finding rather than hiding it."""
+    etaS: the per-call errors add up over many calls of a relaxed state, and
+    the result stays slightly farther from the stencil than leaving etaS
+    unchanged (measured 1.05x the identity's error for the width-32 network
+    with its stored etaS gain, 1.14x for width 16); no etaS gain from 0.01 to
+    1 on other held-out rollouts brought it below the identity
+    (surrogate.calibrate_gain), so the bound records that finding."""
     net = S.load(os.path.join(WEIGHTS_DIR, weights))
     shape = (32, 128, 128)
     state = S.microstructure(shape, seed=515151, vf=0.25)
@@ -71,7 +73,7 @@ def test_many_cycles_per_field_against_the_identity(weights):
     print(f)
     assert f["surrogate"]["etaL"] < 0.6 * f["identity"]["etaL"]
     assert f["surrogate"]["c"] < 0.6 * f["identity"]["c"]
-    assert f["surrogate"]["etaS"] < 2.0 * f["identity"]["etaS"]
+    assert f["surrogate"]["etaS"] < 1.25 * f["identity"]["etaS"]
     assert r["mass_drift"] <= 1e-12 and r["fallbacks"] == 0
 
 

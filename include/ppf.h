@@ -191,6 +191,9 @@ typedef struct ppf_tune {
                             launch (the next step's CTAs are placed while this one's last CTAs
                             finish; every memory access still waits for the previous step);
                             0: plain launches.  Ensembles ignore it. */
+    int sched;           /* 1 (the default): CTAs take work items from a global counter, so that
+                            faster CTAs take more; 0: items dealt round-robin.  Both give the
+                            same bits. */
     double us_per_step;  /* measured time of the winner (ppf_autotune only) */
 } ppf_tune;
 

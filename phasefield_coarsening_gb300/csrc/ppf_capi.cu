@@ -30,6 +30,11 @@ static thread_local char g_err[512];
 // at 256^3, where the step is long against the launch gap).
 static constexpr int kStepPdl = 1;
 
+// CTAs take the step's work items from a global counter (in the same
+// chunk-major order as the round-robin deal), so that CTAs that run faster
+// take more items and the launch's CTAs end closer together.
+static constexpr int kStepSched = 1;
+
 static int seterr(int code, const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -184,6 +189,7 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
     }
     c->stream = c->own;
     c->derr = (int *)(c->dres + 32);
+    c->dsched = c->derr + 4;
     c->wait_limit_ns = 1000000000ULL;
     for (int b = 0; b < 2; ++b)
         for (int f = 0; f < 3; ++f) c->fld[b][f] = (char *)c->state + (size_t)(3 * b + f) * fbytes;
@@ -198,6 +204,7 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
         }
     c->tune.roll = 1;
     c->tune.pdl = kStepPdl;
+    c->tune.sched = kStepSched;
     c->tune.grid = precision == PPF_F32 ? tma_grid<float>(c->g, c->num_sms, &c->tune.zc)
                                         : tma_grid<double>(c->g, c->num_sms, &c->tune.zc);
     if (c->tune.grid < 1) {
@@ -322,7 +329,8 @@ int check_device_error(ppf_ctx *c) {
     CU(cudaMemcpyAsync(&h, c->derr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     if (h) {
-        CU(cudaMemsetAsync(c->derr, 0, sizeof(int), c->stream));
+        // the error word, and the scheduler pair that an abandoned step may leave set
+        CU(cudaMemsetAsync(c->derr, 0, 6 * sizeof(int), c->stream));
         CU(cudaStreamSynchronize(c->stream));
         return seterr(PPF_ETIMEOUT, "a device wait exceeded its limit; the state of that step is invalid");
     }
@@ -334,7 +342,9 @@ static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
     if (nsteps < 0) return seterr(PPF_EINVAL, "negative step count");
     if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
     if (nsteps == 0) return PPF_OK;
-    int rc = ensure_partials(c, 3 * c->tune.grid);
+    const int64_t items = c->prec == PPF_F32 ? tma_items<float>(c->g, c->tune.zc) : tma_items<double>(c->g, c->tune.zc);
+    if (items > ((int64_t)1 << 30)) return seterr(PPF_EINVAL, "too many work items");
+    int rc = ensure_partials(c, 3 * (int)items);
     if (rc) return rc;
     for (int64_t s = 0; s < nsteps; ++s) {
         const bool last = s == nsteps - 1;
@@ -347,17 +357,17 @@ static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
         if (c->prec == PPF_F32) {
             const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
             e = launch_step_tma<float>(c->g, c->kf, m, ff(c, oe, oc), c_only, c->eqA, part, c->tune,
-                                       c->derr, c->wait_limit_ns, inject, c->stream);
+                                       c->derr, c->wait_limit_ns, inject, c->dsched, c->stream);
         } else {
             const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
             e = launch_step_tma<double>(c->g, c->kd, m, fd(c, oe, oc), c_only, c->eqA, part, c->tune,
-                                        c->derr, c->wait_limit_ns, inject, c->stream);
+                                        c->derr, c->wait_limit_ns, inject, c->dsched, c->stream);
         }
         if (e != cudaSuccess) return seterr(PPF_ECUDA, "step launch failed: %s", cudaGetErrorString(e));
         c->cur_eta = oe;
         c->cur_c = oc;
         c->steps++;
-        if (last) CU(launch_final_sum(c->partials, c->tune.grid, 3, c_only ? 1 : 3, c->dres, c->stream));
+        if (last) CU(launch_final_sum(c->partials, (int)items, 3, c_only ? 1 : 3, c->dres, c->stream));
     }
     return PPF_OK;
 }
@@ -428,6 +438,7 @@ extern "C" int ppf_get_tune(const ppf_ctx *c, ppf_tune *t) {
     t->roll = c->tune.roll;
     t->grid = c->tune.grid;
     t->pdl = c->tune.pdl;
+    t->sched = c->tune.sched;
     t->us_per_step = 0.0;
     return PPF_OK;
 }
@@ -437,6 +448,7 @@ extern "C" int ppf_set_tune(ppf_ctx *c, const ppf_tune *t) {
     if (t->roll != 1 && t->roll != 3) return seterr(PPF_EINVAL, "roll must be 1 or 3");
     if (t->zc < 1 || t->zc > c->nz) return seterr(PPF_EINVAL, "zc must be in [1, nz]");
     if (t->pdl != 0 && t->pdl != 1) return seterr(PPF_EINVAL, "pdl must be 0 or 1");
+    if (t->sched != 0 && t->sched != 1) return seterr(PPF_EINVAL, "sched must be 0 or 1");
     CU(cudaStreamSynchronize(c->stream));
     const int grid = grid_for(c, t->zc);
     if (grid < 1) return seterr(PPF_ECUDA, "no launch shape for zc=%d", t->zc);
@@ -444,6 +456,7 @@ extern "C" int ppf_set_tune(ppf_ctx *c, const ppf_tune *t) {
     c->tune.roll = t->roll;
     c->tune.grid = grid;
     c->tune.pdl = t->pdl;
+    c->tune.sched = t->sched;
     return PPF_OK;
 }
 
@@ -451,10 +464,11 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     if (!c) return seterr(PPF_EINVAL, "null context");
     if (!c->uploaded) return seterr(PPF_ESTATE, "autotuning needs an uploaded state");
     if (trial_steps < 1) trial_steps = 1;
-    // candidates: the model's chunk, powers of two, a single chunk, and the
-    // chunks that deal k = 3..7 items to nearly every CTA (so that the
-    // resident CTAs end together); both unrolls; with and without
-    // programmatic dependent launch
+    // candidates: the model's chunk, powers of two and a few short chunks
+    // (fine items for the counter's deal), a single chunk, and the chunks
+    // that deal k = 3..7 items to nearly every CTA (so that the resident
+    // CTAs end together); both unrolls; with and without programmatic
+    // dependent launch; counter or round-robin deal
     int zcs[16], nzc = 0;
     auto add = [&](int z) {
         if (z < 1 || z > c->nz) return;
@@ -465,6 +479,8 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     add(c->tune.zc);
     add(c->nz);
     for (int z = 8; z <= 128; z *= 2) add(z);
+    add(4);
+    add(12);
     add((c->tune.zc + 1) / 2);
     add(c->tune.zc * 2);
     {
@@ -488,10 +504,12 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     CU(cudaEventCreate(&e1));
     float best_ms = -1.0f;
     StepTune win = keep;
+    for (int sd = 1; sd >= 0 && rc == PPF_OK; --sd)
     for (int pdl = 1; pdl >= 0 && rc == PPF_OK; --pdl)
     for (int r = 0; r < 2 && rc == PPF_OK; ++r)
         for (int i = 0; i < nzc && rc == PPF_OK; ++i) {
             StepTune t = keep;
+            t.sched = sd;
             t.pdl = pdl;
             t.roll = r == 0 ? 3 : 1;
             t.zc = zcs[i];
@@ -526,6 +544,7 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
         best->roll = win.roll;
         best->grid = win.grid;
         best->pdl = win.pdl;
+        best->sched = win.sched;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }
     return PPF_OK;

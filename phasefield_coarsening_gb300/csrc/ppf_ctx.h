@@ -23,11 +23,12 @@ struct ppf_ctx {
     void *fld[2][3];      // [buffer][etaS, etaL, c]
     int cur_eta, cur_c;   // buffer holding the current eta / c
     double *staging;      // 3 * cells doubles, compact [z][y][x]
-    double *partials;     // per-CTA partial sums
+    double *partials;     // partial sums (per work item of the step, per block of other kernels)
     int partials_cap;     // in doubles
     double *dres;         // device results: [0..2] increments, [3..7] observables, [8..12] particles,
                           // [16..19] mass-projection plan; the error word follows at dres + 32
     int *derr;            // device error word set by a kernel whose bounded wait ran out
+    int *dsched;          // the step's scheduler word pair (dres + 32, after the error word)
     CUtensorMap maps[2][3];   // TMA maps of the fields of both buffers
     ppf::StepTune tune;        // launch choices of the fused step (grid, z chunk, unroll)
     unsigned long long wait_limit_ns;

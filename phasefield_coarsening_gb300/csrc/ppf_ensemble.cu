@@ -68,6 +68,8 @@ struct ppf_ensemble {
     double *partials;            // 3 doubles per work item
     int partials_cap;
     int items, grid, zc, roll;
+    int sched;                   // 1: work items from a counter (domain 0's scheduler pair; the
+                                 // ensemble's stream orders every domain's launches)
     int parity;                  // buffer holding the current state of every domain
     int64_t steps;
     cudaStream_t stream;
@@ -127,11 +129,11 @@ static int launch_one(ppf_ensemble *e, bool stats) {
     if (e->prec == PPF_F32)
         r = launch_step_multi<float>(e->dtable, e->n, e->items, c0->kf, false, e->eqA, e->parity,
                                      stats ? e->partials : nullptr, e->grid, e->roll, c0->derr, c0->wait_limit_ns,
-                                     e->stream);
+                                     e->sched ? c0->dsched : nullptr, e->stream);
     else
         r = launch_step_multi<double>(e->dtable, e->n, e->items, c0->kd, false, e->eqA, e->parity,
                                       stats ? e->partials : nullptr, e->grid, e->roll, c0->derr, c0->wait_limit_ns,
-                                      e->stream);
+                                      e->sched ? c0->dsched : nullptr, e->stream);
     if (r != cudaSuccess) return err_(PPF_ECUDA, "ensemble step launch: %s", cudaGetErrorString(r));
     e->parity ^= 1;
     return PPF_OK;
@@ -180,6 +182,7 @@ extern "C" int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, 
     e->bc = bc;
     e->zc = 32;
     e->roll = 1;
+    e->sched = 1;
     int rc = PPF_OK;
     for (int d = 0; d < n && rc == PPF_OK; ++d) {
         ppf_ctx *c = nullptr;
@@ -314,6 +317,7 @@ extern "C" int ppf_ensemble_get_tune(const ppf_ensemble *e, ppf_tune *t) {
     t->roll = e->roll;
     t->grid = e->grid;
     t->pdl = 0;
+    t->sched = e->sched;
     t->us_per_step = 0;
     return PPF_OK;
 }
@@ -322,9 +326,11 @@ extern "C" int ppf_ensemble_set_tune(ppf_ensemble *e, const ppf_tune *t) {
     if (!e || !t) return err_(PPF_EINVAL, "null argument");
     if (t->roll != 1 && t->roll != 3) return err_(PPF_EINVAL, "roll must be 1 or 3");
     if (t->zc < 1) return err_(PPF_EINVAL, "zc must be >= 1");
+    if (t->sched != 0 && t->sched != 1) return err_(PPF_EINVAL, "sched must be 0 or 1");
     ECU(cudaStreamSynchronize(e->stream));
     e->zc = t->zc;
     e->roll = t->roll;
+    e->sched = t->sched;
     return build_table(e);
 }
 
@@ -337,18 +343,20 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
     // keep every domain's state: save it, try the choices, restore it
     for (ppf_ctx *x : e->dom)
         if ((rc = do_unpack(x)) != PPF_OK) return rc;
-    const int zcs[] = {8, 16, 24, 32, 48, 64, 128};
-    const int keep_zc = e->zc, keep_roll = e->roll;
+    const int zcs[] = {4, 8, 12, 16, 24, 32, 48, 64, 128};
+    const int keep_zc = e->zc, keep_roll = e->roll, keep_sched = e->sched;
     const int64_t keep_steps = e->steps;
-    int best_zc = keep_zc, best_roll = keep_roll;
+    int best_zc = keep_zc, best_roll = keep_roll, best_sched = keep_sched;
     float best_ms = -1.0f;
     cudaEvent_t t0, t1;
     ECU(cudaEventCreate(&t0));
     ECU(cudaEventCreate(&t1));
+    for (int sd = 1; sd >= 0 && rc == PPF_OK; --sd)
     for (int r = 0; r < 2 && rc == PPF_OK; ++r)
         for (int zc : zcs) {
             e->zc = zc;
             e->roll = r == 0 ? 1 : 3;
+            e->sched = sd;
             if ((rc = build_table(e)) != PPF_OK) break;
             for (int s = 0; s < 2 && rc == PPF_OK; ++s) rc = launch_one(e, false);     // warm-up
             if (rc) break;
@@ -359,12 +367,13 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
             if ((rc = check_device_error(e->dom[0])) != PPF_OK) break;
             float ms = 0;
             cudaEventElapsedTime(&ms, t0, t1);
-            if (best_ms < 0 || ms < best_ms) { best_ms = ms; best_zc = e->zc; best_roll = e->roll; }
+            if (best_ms < 0 || ms < best_ms) { best_ms = ms; best_zc = e->zc; best_roll = e->roll; best_sched = e->sched; }
         }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     e->zc = rc == PPF_OK ? best_zc : keep_zc;
     e->roll = rc == PPF_OK ? best_roll : keep_roll;
+    e->sched = rc == PPF_OK ? best_sched : keep_sched;
     int rc2 = build_table(e);
     for (ppf_ctx *x : e->dom)
         if (rc2 == PPF_OK) {
@@ -382,6 +391,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
         best->roll = e->roll;
         best->grid = e->grid;
         best->pdl = 0;
+        best->sched = e->sched;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }
     return PPF_OK;

@@ -6,12 +6,14 @@ namespace ppf {
 template void step_tile<float>(int *, int *);
 template int tma_grid_items<float>(int64_t, int);
 template cudaError_t launch_step_multi<float>(const DomainDesc *, int, int, const Coef<float> &, bool, bool, int,
-                                            double *, int, int, int *, unsigned long long, cudaStream_t);
+                                            double *, int, int, int *, unsigned long long, int *,
+                                            cudaStream_t);
 template int make_field_map<float>(const Geom &, const float *, CUtensorMap *);
 template int tma_grid<float>(const Geom &, int, int *);
 template int tma_grid_for_zc<float>(const Geom &, int, int);
+template int64_t tma_items<float>(const Geom &, int);
 template cudaError_t launch_step_tma<float>(const Geom &, const Coef<float> &, const CUtensorMap *, Fields<float>, bool,
-                                          bool, double *, const StepTune &, int *, unsigned long long, int,
+                                          bool, double *, const StepTune &, int *, unsigned long long, int, int *,
                                           cudaStream_t);
 
 }  // namespace ppf

@@ -6,12 +6,14 @@ namespace ppf {
 template void step_tile<double>(int *, int *);
 template int tma_grid_items<double>(int64_t, int);
 template cudaError_t launch_step_multi<double>(const DomainDesc *, int, int, const Coef<double> &, bool, bool, int,
-                                            double *, int, int, int *, unsigned long long, cudaStream_t);
+                                            double *, int, int, int *, unsigned long long, int *,
+                                            cudaStream_t);
 template int make_field_map<double>(const Geom &, const double *, CUtensorMap *);
 template int tma_grid<double>(const Geom &, int, int *);
 template int tma_grid_for_zc<double>(const Geom &, int, int);
+template int64_t tma_items<double>(const Geom &, int);
 template cudaError_t launch_step_tma<double>(const Geom &, const Coef<double> &, const CUtensorMap *, Fields<double>, bool,
-                                          bool, double *, const StepTune &, int *, unsigned long long, int,
+                                          bool, double *, const StepTune &, int *, unsigned long long, int, int *,
                                           cudaStream_t);
 
 }  // namespace ppf

@@ -358,7 +358,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     const __grid_constant__ CUtensorMap mapC, Geom g1, Coef<T> k, CoefV<T> kv, Fields<T> out1,
                     int ntx1, int nty1,
                     int zc1, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
-                    int inject_stall, const DomainDesc *__restrict__ table, int ndom, int mitems, int parity) {
+                    int inject_stall, const DomainDesc *__restrict__ table, int ndom, int mitems, int parity,
+                    int *__restrict__ sched) {
     using G = TmaGeo<T>;
     constexpr int TX = G::TX, TY = G::TY, S = G::S, XH = G::XH, BX = G::BX, CY = G::CY;
     extern __shared__ __align__(128) unsigned char smem_dyn[];
@@ -408,17 +409,46 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const int m_above = MmLay<T>::row(ty0 - 1, tx + XH), m_below = MmLay<T>::row(ty0 + CY, tx + XH);
 
     double acc[3] = {0.0, 0.0, 0.0};
-    if ((int)blockIdx.x < nitems) {
+    __shared__ int s_next[2];
+    // (with the scheduler every CTA takes part, so that the count of CTAs
+    // that stopped taking items reaches the grid size)
+    if (sched || (int)blockIdx.x < nitems) {
         if (tid == 0) {
             for (int s = 0; s < S; ++s) mbar_init(smem_u32(&sm.bar[s]), 1);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
-        __syncthreads();
 
-        // producer (thread 0): walks the same items and planes as the consumers,
-        // S-2 loads ahead
-        int p_item = blockIdx.x, p_pz = 0, p_xs = 0, p_ys = 0;
+        // producer (thread 0): takes the CTA's items and walks their planes,
+        // S-2 loads ahead of the consumers.  Items come round-robin
+        // (blockIdx.x, + gridDim.x, ...) or, with a scheduler word pair, from
+        // a global counter in the same chunk-major order, so that a CTA that
+        // runs faster takes more items.  Each item id is published in s_next
+        // (two slots: an item spans at least three planes, so the producer is
+        // never more than one item ahead), written at least two plane
+        // barriers before the consumers read it.
+        int p_item = 0, p_pz = 0, p_xs = 0, p_ys = 0, p_seq = 0;
+        bool p_done = sched == nullptr;           // stopped taking items (dynamic mode)
+        auto take = [&]() {
+            int v;
+            if (sched) {
+                v = atomicAdd(&sched[0], 1);
+                if (v >= nitems) {
+                    v = nitems;
+                    // the last CTA to stop taking items resets the pair for the next launch
+                    if (atomicAdd(&sched[1], 1) == (int)gridDim.x - 1) {
+                        atomicExch(&sched[0], 0);
+                        atomicExch(&sched[1], 0);
+                    }
+                    p_done = true;
+                }
+            } else {
+                v = p_seq == 0 ? (int)blockIdx.x : min(nitems, p_item + (int)gridDim.x);
+            }
+            s_next[p_seq & 1] = v;
+            ++p_seq;
+            p_item = v;
+        };
         const CUtensorMap *p_mS = &mapS, *p_mL = &mapL, *p_mC = &mapC;
         Item p_it;
         auto p_set = [&]() {
@@ -439,7 +469,6 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 }
             }
         };
-        p_set();
         int ist = 0, issued = 0;
         auto issue = [&]() {
             const uint32_t bar = smem_u32(&sm.bar[ist]);
@@ -451,14 +480,18 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             tma_load_3d(smem_u32(sm.raw[ist][1]), p_mL, p_xs, p_ys, zs, bar);
             tma_load_3d(smem_u32(sm.raw[ist][2]), p_mC, p_xs, p_ys, zs, bar);
             if (++p_pz > p_it.z1) {
-                p_item += gridDim.x;
+                take();
                 p_set();
             }
             ist = ist + 1 == S ? 0 : ist + 1;
             ++issued;
         };
-        if (tid == 0)
+        if (tid == 0) {
+            take();
+            p_set();
             for (int l = 0; l < S - 2 && p_item < nitems; ++l) issue();
+        }
+        __syncthreads();                              // barriers initialised, first item published
 
         // three register planes whose roles rotate: q-1, q, q+1
         constexpr int H = CY / 2;
@@ -474,7 +507,9 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
         uint32_t par = 0;
         int st_prev = 0, mb_prev = 0;
         bool dead = false;
-        for (int item = blockIdx.x; item < nitems && !dead; item += gridDim.x) {
+        for (int seq = 0; !dead; ++seq) {
+            const int item = s_next[seq & 1];
+            if (item >= nitems) break;
             const Item it = item_at<MULTI>(item, ntiles1, zc1, g1.nz, table, ndom);
             const Geom g = MULTI ? table[it.dom].g : g1;
             Fields<T> out = out1;
@@ -695,8 +730,9 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     RB = RC;
                 }
             }
-            if (MULTI && STATS && !dead) {
-                // ensemble: the increment sums of each work item (its domain's)
+            if (STATS && !dead) {
+                // the increment sums of each work item, summed later in item order
+                // (the same bits whichever CTA took the item)
                 __shared__ double ired[TmaGeo<T>::NT / 32][3];
                 __syncthreads();
 #pragma unroll
@@ -717,30 +753,17 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             }
         }
         if (dead) {
-            // drain this CTA's own copies still in flight (bounded), then leave
-            if (tid == 0)
+            // drain this CTA's own copies still in flight (bounded), stop taking
+            // items (the remaining CTAs then reset the scheduler pair), leave
+            if (tid == 0) {
                 for (int d = 0; d < issued - consumed; ++d)
                     (void)mbar_wait(smem_u32(&sm.bar[(st + d) % S]), par ^ (uint32_t)(((st + d) / S) & 1), limit_ns);
-            return;
-        }
-    }
-    if (STATS && !MULTI) {
-        // block sum -> partials[blockIdx.x * 3 + i]
-        __shared__ double red[TmaGeo<T>::NT / 32][3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            double v = acc[i];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) red[warp][i] = v;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            for (int i = 0; i < 3; ++i) {
-                double s = 0;
-                for (int w = 0; w < TmaGeo<T>::NT / 32; ++w) s += red[w][i];
-                partials[(int64_t)blockIdx.x * 3 + i] = s;
+                if (!p_done && atomicAdd(&sched[1], 1) == (int)gridDim.x - 1) {
+                    atomicExch(&sched[0], 0);
+                    atomicExch(&sched[1], 0);
+                }
             }
+            return;
         }
     }
 }
@@ -877,6 +900,14 @@ int tma_grid_for_zc(const Geom &g, int num_sms, int zc) {
     return (int)(items < slots ? items : slots);
 }
 
+template <typename T>
+int64_t tma_items(const Geom &g, int zc) {
+    using G = TmaGeo<T>;
+    if (zc < 1) zc = 1;
+    if (zc > g.nz) zc = g.nz;
+    return (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY) * ((g.nz + zc - 1) / zc);
+}
+
 // A launch of the single-domain step; with `pdl` the launch allows
 // programmatic dependent launch (the kernel's griddepcontrol.wait keeps the
 // stream order for every global memory access).
@@ -900,7 +931,7 @@ static void launch_step_ex(bool pdl, void (*kern)(KArgs...), int grid, int block
 template <typename T, int R, bool FULL>
 static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only, bool eqA,
                      double *partials, const StepTune &tune, int *err, unsigned long long limit_ns, int inject_stall,
-                     cudaStream_t s) {
+                     int *sched, cudaStream_t s) {
     using G = TmaGeo<T>;
     const int ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
     const size_t sh = tma_smem_bytes<T>();
@@ -910,7 +941,7 @@ static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, F
 #define PPF_LAUNCH(ST, CO, EQ)                                                                                        \
     launch_step_ex(tune.pdl != 0, step_tma_kernel<T, ST, CO, EQ, R, false, FULL>, tune.grid, G::NT, sh, s, maps[0],   \
                    maps[1], maps[2], g, k, kv, out, ntx, nty, tune.zc, partials, err, limit_ns, inject_stall,        \
-                   no_table, 0, 0, 0)
+                   no_table, 0, 0, 0, tune.sched ? sched : nullptr)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -924,16 +955,16 @@ static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, F
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
                             bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
-                            int inject_stall, cudaStream_t s) {
+                            int inject_stall, int *sched, cudaStream_t s) {
     using G = TmaGeo<T>;
     // FULL: every tile inside the domain, and every element offset below 2^32
     const bool full = g.nx % G::TX == 0 && g.ny % G::TY == 0 && g.total <= ((int64_t)1 << 32);
     if (tune.roll == 1) {
-        if (full) launch_r<T, 1, true>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, s);
-        else launch_r<T, 1, false>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, s);
+        if (full) launch_r<T, 1, true>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
+        else launch_r<T, 1, false>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
     } else {
-        if (full) launch_r<T, 3, true>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, s);
-        else launch_r<T, 3, false>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, s);
+        if (full) launch_r<T, 3, true>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
+        else launch_r<T, 3, false>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
     }
     return cudaGetLastError();
 }
@@ -941,7 +972,7 @@ cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *
 template <typename T, int R>
 static void launch_multi_r(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
                            int parity, double *partials, int grid, int *err, unsigned long long limit_ns,
-                           cudaStream_t s) {
+                           int *sched, cudaStream_t s) {
     using G = TmaGeo<T>;
     const size_t sh = tma_smem_bytes<T>();
     const bool st = partials != nullptr;
@@ -954,7 +985,7 @@ static void launch_multi_r(const DomainDesc *table, int ndom, int items, const C
 #define PPF_LAUNCH(ST, CO, EQ)                                                                                       \
     step_tma_kernel<T, ST, CO, EQ, R, true, false><<<grid, G::NT, sh, s>>>(none, none, none, g0, k, kv, o0, 1, 1, 1, \
                                                                            partials, err, limit_ns, 0, table, ndom, \
-                                                                           items, parity)
+                                                                           items, parity, sched)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -968,9 +999,9 @@ static void launch_multi_r(const DomainDesc *table, int ndom, int items, const C
 template <typename T>
 cudaError_t launch_step_multi(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
                               int parity, double *partials, int grid, int roll, int *err,
-                              unsigned long long limit_ns, cudaStream_t s) {
-    if (roll == 1) launch_multi_r<T, 1>(table, ndom, items, k, c_only, eqA, parity, partials, grid, err, limit_ns, s);
-    else launch_multi_r<T, 3>(table, ndom, items, k, c_only, eqA, parity, partials, grid, err, limit_ns, s);
+                              unsigned long long limit_ns, int *sched, cudaStream_t s) {
+    if (roll == 1) launch_multi_r<T, 1>(table, ndom, items, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, s);
+    else launch_multi_r<T, 3>(table, ndom, items, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, s);
     return cudaGetLastError();
 }
 

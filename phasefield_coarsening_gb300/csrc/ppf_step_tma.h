@@ -25,6 +25,7 @@ struct StepTune {
     int zc;     // z planes per work item
     int roll;   // 3: plane body unrolled three times; 1: one copy
     int pdl;    // 1: consecutive launches overlap by programmatic dependent launch
+    int sched;  // 1: CTAs take work items from a global counter; 0: round-robin
 };
 
 // Tensor map of one padded field (3-D: x pitch, ny+2 rows, nz+2 planes)
@@ -43,13 +44,20 @@ int tma_grid_for_zc(const Geom &g, int num_sms, int zc);
 
 // One fused step.  maps = {etaS, etaL, c} of the input state; eqA selects
 // the specialisation for AS == AL (mu needs no reciprocal); `partials`
-// (nullable) receives 3 doubles per CTA; `err` is a device word that a
-// CTA sets when an mbarrier wait exceeds limit_ns.  inject_stall != 0 is a
-// test hook that makes one wait per CTA run out.
+// (nullable) receives 3 doubles per work item (tma_items of them); `err` is
+// a device word that a CTA sets when an mbarrier wait exceeds limit_ns.
+// inject_stall != 0 is a test hook that makes one wait per CTA run out.
+// `sched` is the launch's scheduler word pair (two ints, zero before the
+// first launch; every launch leaves them zero), used when tune.sched is set;
+// launches that share a pair must be ordered on one stream.
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
                             bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
-                            int inject_stall, cudaStream_t s);
+                            int inject_stall, int *sched, cudaStream_t s);
+
+// Work items of one single-domain step with z chunk zc.
+template <typename T>
+int64_t tma_items(const Geom &g, int zc);
 
 // Tiles of the fused step (x, y), for sizing ensemble work items.
 template <typename T>
@@ -61,10 +69,11 @@ int tma_grid_items(int64_t items, int num_sms);
 
 // One fused step of every domain of an ensemble: reads buffer `parity` of
 // each domain and writes buffer 1-parity.  `partials` (nullable) receives 3
-// doubles per work item (the last-step increment sums).
+// doubles per work item (the last-step increment sums); `sched` (nullable)
+// as for launch_step_tma.
 template <typename T>
 cudaError_t launch_step_multi(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
                               int parity, double *partials, int grid, int roll, int *err,
-                              unsigned long long limit_ns, cudaStream_t s);
+                              unsigned long long limit_ns, int *sched, cudaStream_t s);
 
 }  // namespace ppf

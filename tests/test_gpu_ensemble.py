@@ -22,9 +22,12 @@ def _single(shape, state, steps, bc, precision, pieces=(37,)):
 
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 @pytest.mark.parametrize("bc", ["periodic", "noflux"])
-def test_ensemble_equals_independent_domains(precision, bc):
+@pytest.mark.parametrize("sched", [1, 0])
+def test_ensemble_equals_independent_domains(precision, bc, sched):
+    """With work items from the counter (1) or dealt round-robin (0)."""
     states = [smooth_state(sh, seed=30 + i) for i, sh in enumerate(SHAPES)]
     with ppf.Ensemble(SHAPES, bc=bc, precision=precision) as e:
+        e.set_tune(8, 1, sched)
         for d, st in enumerate(states):
             e.upload(d, *st)
         e.step(1)          # leaves every domain at buffer 1

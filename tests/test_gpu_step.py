@@ -258,23 +258,35 @@ def test_ppf_program_matches_reference_run(name, tmp_path):
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 def test_launch_choices_are_bit_identical(precision):
-    """The z chunk and the unroll change only who computes a cell, never the
-    arithmetic: every launch choice gives the same bits."""
+    """The z chunk, the unroll, the launch overlap and the way CTAs take work
+    items (counter or round-robin) change only who computes a cell, never the
+    arithmetic: every launch choice gives the same bits.  The last step's
+    increment sums are summed per work item in item order, so for one z
+    chunk they are the same bits whichever CTA took which item; another z
+    chunk groups the same terms differently."""
     shape = (40, 35, 70)
     st = smooth_state(shape, seed=12)
-    ref = None
-    for zc, roll, pdl in [(None, None, None), (1, 3, 1), (7, 1, 0), (40, 3, 0), (13, 1, 1)]:
+    ref, inc_of = None, {}
+    for zc, roll, pdl, sched in [(None, None, None, None), (1, 3, 1, 1), (1, 1, 0, 0), (7, 1, 0, 0), (7, 3, 1, 1),
+                                 (40, 3, 0, 1), (40, 1, 1, 0), (13, 1, 1, 0), (13, 3, 0, 1), (2, 1, 1, 1)]:
         with ppf.Simulation(shape, bc=1, precision=precision) as s:
             if zc is not None:
-                s.set_tune(zc, roll, pdl)
+                s.set_tune(zc, roll, pdl, sched)
             s.upload(*st)
-            s.step(6)
+            for _ in range(3):            # several launches: every launch resets the counter
+                s.step(2)
+            red = s.reduce()
             out = s.download()
+            inc = (red["sum_dc2"], red["sum_detaS2"], red["sum_detaL2"])
         if ref is None:
-            ref = out
+            ref, ref_inc = out, inc
         else:
             for a, b in zip(out, ref):
-                assert np.array_equal(a, b), (zc, roll, pdl)
+                assert np.array_equal(a, b), (zc, roll, pdl, sched)
+            np.testing.assert_allclose(inc, ref_inc, rtol=1e-13)
+            if zc in inc_of:
+                assert inc == inc_of[zc], (zc, roll, pdl, sched)
+            inc_of[zc] = inc
 
 
 def test_autotune_keeps_state_and_picks_a_valid_choice():

@@ -194,6 +194,10 @@ typedef struct ppf_tune {
     int sched;           /* 1 (the default): CTAs take work items from a global counter, so that
                             faster CTAs take more; 0: items dealt round-robin.  Both give the
                             same bits. */
+    int zc2;             /* > 0 and < zc: the top `tail` planes are cut into work items of zc2
+                            planes instead of zc (short items end the step, so that its CTAs end
+                            closer together); 0: every item zc planes */
+    int tail;
     double us_per_step;  /* measured time of the winner (ppf_autotune only) */
 } ppf_tune;
 

@@ -342,7 +342,7 @@ static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
     if (nsteps < 0) return seterr(PPF_EINVAL, "negative step count");
     if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
     if (nsteps == 0) return PPF_OK;
-    const int64_t items = c->prec == PPF_F32 ? tma_items<float>(c->g, c->tune.zc) : tma_items<double>(c->g, c->tune.zc);
+    const int64_t items = c->prec == PPF_F32 ? tma_items<float>(c->g, c->tune) : tma_items<double>(c->g, c->tune);
     if (items > ((int64_t)1 << 30)) return seterr(PPF_EINVAL, "too many work items");
     int rc = ensure_partials(c, 3 * (int)items);
     if (rc) return rc;
@@ -427,9 +427,15 @@ extern "C" int ppf_debug_inject(ppf_ctx *c, int fault) {
     return PPF_OK;
 }
 
+static int grid_for(ppf_ctx *c, const StepTune &t) {
+    return c->prec == PPF_F32 ? tma_grid_for<float>(c->g, c->num_sms, t) : tma_grid_for<double>(c->g, c->num_sms, t);
+}
+
 static int grid_for(ppf_ctx *c, int zc) {
-    return c->prec == PPF_F32 ? tma_grid_for_zc<float>(c->g, c->num_sms, zc)
-                              : tma_grid_for_zc<double>(c->g, c->num_sms, zc);
+    StepTune t = c->tune;
+    t.zc = zc;
+    t.zc2 = t.tail = 0;
+    return grid_for(c, t);
 }
 
 extern "C" int ppf_get_tune(const ppf_ctx *c, ppf_tune *t) {
@@ -439,6 +445,8 @@ extern "C" int ppf_get_tune(const ppf_ctx *c, ppf_tune *t) {
     t->grid = c->tune.grid;
     t->pdl = c->tune.pdl;
     t->sched = c->tune.sched;
+    t->zc2 = c->tune.zc2;
+    t->tail = c->tune.tail;
     t->us_per_step = 0.0;
     return PPF_OK;
 }
@@ -449,14 +457,18 @@ extern "C" int ppf_set_tune(ppf_ctx *c, const ppf_tune *t) {
     if (t->zc < 1 || t->zc > c->nz) return seterr(PPF_EINVAL, "zc must be in [1, nz]");
     if (t->pdl != 0 && t->pdl != 1) return seterr(PPF_EINVAL, "pdl must be 0 or 1");
     if (t->sched != 0 && t->sched != 1) return seterr(PPF_EINVAL, "sched must be 0 or 1");
+    if (t->zc2 < 0 || t->tail < 0 || t->tail > c->nz) return seterr(PPF_EINVAL, "need zc2 >= 0 and 0 <= tail <= nz");
     CU(cudaStreamSynchronize(c->stream));
-    const int grid = grid_for(c, t->zc);
-    if (grid < 1) return seterr(PPF_ECUDA, "no launch shape for zc=%d", t->zc);
-    c->tune.zc = t->zc;
-    c->tune.roll = t->roll;
-    c->tune.grid = grid;
-    c->tune.pdl = t->pdl;
-    c->tune.sched = t->sched;
+    StepTune n = c->tune;
+    n.zc = t->zc;
+    n.roll = t->roll;
+    n.pdl = t->pdl;
+    n.sched = t->sched;
+    n.zc2 = t->zc2 < t->zc ? t->zc2 : 0;
+    n.tail = n.zc2 > 0 ? t->tail : 0;
+    n.grid = grid_for(c, n);
+    if (n.grid < 1) return seterr(PPF_ECUDA, "no launch shape for zc=%d", t->zc);
+    c->tune = n;
     return PPF_OK;
 }
 
@@ -504,6 +516,23 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     CU(cudaEventCreate(&e1));
     float best_ms = -1.0f;
     StepTune win = keep;
+    auto trial = [&](StepTune t) {
+        t.grid = grid_for(c, t);
+        if (t.grid < 1) return;
+        c->tune = t;
+        if ((rc = run_steps(c, 2, false)) != PPF_OK) return;      // warm-up
+        if (cudaEventRecord(e0, c->stream) != cudaSuccess) { rc = seterr(PPF_ECUDA, "event record"); return; }
+        if ((rc = run_steps(c, trial_steps, false)) != PPF_OK) return;
+        if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = seterr(PPF_ECUDA, "event timing failed");
+            return;
+        }
+        if ((rc = check_device_error(c)) != PPF_OK) return;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (best_ms < 0 || ms < best_ms) { best_ms = ms; win = t; }
+    };
+    // uniform chunks
     for (int sd = 1; sd >= 0 && rc == PPF_OK; --sd)
     for (int pdl = 1; pdl >= 0 && rc == PPF_OK; --pdl)
     for (int r = 0; r < 2 && rc == PPF_OK; ++r)
@@ -513,21 +542,39 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
             t.pdl = pdl;
             t.roll = r == 0 ? 3 : 1;
             t.zc = zcs[i];
-            t.grid = grid_for(c, t.zc);
-            if (t.grid < 1) continue;
-            c->tune = t;
-            if ((rc = run_steps(c, 2, false)) != PPF_OK) break;      // warm-up
-            if (cudaEventRecord(e0, c->stream) != cudaSuccess) { rc = seterr(PPF_ECUDA, "event record"); break; }
-            if ((rc = run_steps(c, trial_steps, false)) != PPF_OK) break;
-            if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
-                rc = seterr(PPF_ECUDA, "event timing failed");
-                break;
-            }
-            if ((rc = check_device_error(c)) != PPF_OK) break;
-            float ms = 0.0f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (best_ms < 0 || ms < best_ms) { best_ms = ms; win = t; }
+            t.zc2 = t.tail = 0;
+            trial(t);
         }
+    // with the counter's deal: longer main chunks (the winner's and longer
+    // ones, which pay fewer halo planes) with chunks of a half to a quarter
+    // of their length at the top of z, covering about one or two waves of
+    // the persistent grid's items
+    if (rc == PPF_OK && win.sched == 1) {
+        const StepTune base = win;
+        int tx = 0, ty = 0;
+        if (c->prec == PPF_F32) step_tile<float>(&tx, &ty);
+        else step_tile<double>(&tx, &ty);
+        const int64_t ntiles = (int64_t)((c->nx + tx - 1) / tx) * ((c->ny + ty - 1) / ty);
+        const int64_t slots = grid_for(c, 1);
+        int mains[5], nm = 0;
+        for (int z : {base.zc, 2 * base.zc, 16, 24, 32}) {
+            if (z < 4 || z > c->nz) continue;
+            bool dup = false;
+            for (int i = 0; i < nm; ++i) dup = dup || mains[i] == z;
+            if (!dup) mains[nm++] = z;
+        }
+        for (int m = 0; m < nm && rc == PPF_OK; ++m)
+            for (int q = 2; q <= 4 && rc == PPF_OK; ++q)
+                for (int waves = 1; waves <= 2 && rc == PPF_OK; ++waves) {
+                    StepTune t = base;
+                    t.zc = mains[m];
+                    t.zc2 = t.zc / q > 1 ? t.zc / q : 2;
+                    const int64_t chunks = (waves * slots + ntiles - 1) / ntiles;
+                    t.tail = (int)(chunks * t.zc2 < c->nz ? chunks * t.zc2 : c->nz / 2);
+                    if (t.zc2 >= t.zc || t.tail < 1) continue;
+                    trial(t);
+                }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->tune = rc == PPF_OK ? win : keep;
@@ -545,6 +592,8 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
         best->grid = win.grid;
         best->pdl = win.pdl;
         best->sched = win.sched;
+        best->zc2 = win.zc2;
+        best->tail = win.tail;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }
     return PPF_OK;

@@ -318,6 +318,7 @@ extern "C" int ppf_ensemble_get_tune(const ppf_ensemble *e, ppf_tune *t) {
     t->grid = e->grid;
     t->pdl = 0;
     t->sched = e->sched;
+    t->zc2 = t->tail = 0;
     t->us_per_step = 0;
     return PPF_OK;
 }
@@ -392,6 +393,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
         best->grid = e->grid;
         best->pdl = 0;
         best->sched = e->sched;
+        best->zc2 = best->tail = 0;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }
     return PPF_OK;

@@ -10,8 +10,8 @@ template cudaError_t launch_step_multi<float>(const DomainDesc *, int, int, cons
                                             cudaStream_t);
 template int make_field_map<float>(const Geom &, const float *, CUtensorMap *);
 template int tma_grid<float>(const Geom &, int, int *);
-template int tma_grid_for_zc<float>(const Geom &, int, int);
-template int64_t tma_items<float>(const Geom &, int);
+template int tma_grid_for<float>(const Geom &, int, const StepTune &);
+template int64_t tma_items<float>(const Geom &, const StepTune &);
 template cudaError_t launch_step_tma<float>(const Geom &, const Coef<float> &, const CUtensorMap *, Fields<float>, bool,
                                           bool, double *, const StepTune &, int *, unsigned long long, int, int *,
                                           cudaStream_t);

@@ -10,8 +10,8 @@ template cudaError_t launch_step_multi<double>(const DomainDesc *, int, int, con
                                             cudaStream_t);
 template int make_field_map<double>(const Geom &, const double *, CUtensorMap *);
 template int tma_grid<double>(const Geom &, int, int *);
-template int tma_grid_for_zc<double>(const Geom &, int, int);
-template int64_t tma_items<double>(const Geom &, int);
+template int tma_grid_for<double>(const Geom &, int, const StepTune &);
+template int64_t tma_items<double>(const Geom &, const StepTune &);
 template cudaError_t launch_step_tma<double>(const Geom &, const Coef<double> &, const CUtensorMap *, Fields<double>, bool,
                                           bool, double *, const StepTune &, int *, unsigned long long, int, int *,
                                           cudaStream_t);

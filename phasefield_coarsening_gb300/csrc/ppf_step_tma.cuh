@@ -320,18 +320,27 @@ struct Item {
     int dom, tile, z0, z1;
 };
 
+// How a single domain's z range is cut into work-item chunks: n1 chunks of
+// zc planes, then chunks of zc2 planes up to nz (the last one may be
+// shorter).  Shorter chunks at the top of z make the last items of a step
+// short, so that the CTAs end closer together.
+struct ZSplit {
+    int zc, zc2, n1;
+};
+
 // Work item `item` of the launch.  Single domain: (z chunk, tile) in
 // chunk-major order.  Ensemble (MULTI): the items of each domain are
 // contiguous, chunk-major within the domain.
 template <bool MULTI>
-__device__ __forceinline__ Item item_at(int item, int ntiles, int zc, int nz, const DomainDesc *table, int ndom) {
+__device__ __forceinline__ Item item_at(int item, int ntiles, const ZSplit &zs, int nz, const DomainDesc *table,
+                                        int ndom) {
     Item it;
     if (!MULTI) {
         const int c = item / ntiles;
         it.dom = 0;
         it.tile = item - c * ntiles;
-        it.z0 = c * zc;
-        it.z1 = min(nz, it.z0 + zc);
+        it.z0 = c < zs.n1 ? c * zs.zc : zs.n1 * zs.zc + (c - zs.n1) * zs.zc2;
+        it.z1 = min(nz, it.z0 + (c < zs.n1 ? zs.zc : zs.zc2));
         return it;
     }
     int lo = 0, hi = ndom - 1;                 // last domain with item0 <= item
@@ -357,7 +366,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
                     const __grid_constant__ CUtensorMap mapC, Geom g1, Coef<T> k, CoefV<T> kv, Fields<T> out1,
                     int ntx1, int nty1,
-                    int zc1, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
+                    ZSplit zs1, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
                     int inject_stall, const DomainDesc *__restrict__ table, int ndom, int mitems, int parity,
                     int *__restrict__ sched) {
     using G = TmaGeo<T>;
@@ -380,7 +389,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const int tx = (warp % G::WX) * 32 + lane;        // own column in the tile
     const int ty0 = (warp / G::WX) * CY;              // first own row in the tile
     const int ntiles1 = ntx1 * nty1;
-    const int nitems = MULTI ? mitems : ntiles1 * ((g1.nz + zc1 - 1) / zc1);
+    const int nitems = mitems;
     const int ob = (ty0 + 1) * BX + tx + XH;          // shared offset of the first own cell
     static_assert(!(MULTI && FULL), "ensembles take the general path");
     // the pair of cells of the one-cell ring around the tile that this thread
@@ -408,7 +417,12 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const int pofs = MmLay<T>::pair((warp / G::WX) * (CY / 2), tx + XH);
     const int m_above = MmLay<T>::row(ty0 - 1, tx + XH), m_below = MmLay<T>::row(ty0 + CY, tx + XH);
 
-    double acc[3] = {0.0, 0.0, 0.0};
+    // increment sums of the statistics step: per thread and work item in the
+    // state's precision (packed, one FMA per pair; FP32: at most 2 zc squares
+    // per lane), then in FP64 across lanes, warps and items
+    V2<T> acc[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) acc[i] = splat(T(0));
     __shared__ int s_next[2];
     // (with the scheduler every CTA takes part, so that the count of CTAs
     // that stopped taking items reaches the grid size)
@@ -453,7 +467,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
         Item p_it;
         auto p_set = [&]() {
             if (p_item < nitems) {
-                p_it = item_at<MULTI>(p_item, ntiles1, zc1, g1.nz, table, ndom);
+                p_it = item_at<MULTI>(p_item, ntiles1, zs1, g1.nz, table, ndom);
                 p_pz = p_it.z0 - 1;
                 // the item's box corner: storage x of the box start (16-byte
                 // aligned) and storage y of interior row y0-1
@@ -510,7 +524,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
         for (int seq = 0; !dead; ++seq) {
             const int item = s_next[seq & 1];
             if (item >= nitems) break;
-            const Item it = item_at<MULTI>(item, ntiles1, zc1, g1.nz, table, ndom);
+            const Item it = item_at<MULTI>(item, ntiles1, zs1, g1.nz, table, ndom);
             const Geom g = MULTI ? table[it.dom].g : g1;
             Fields<T> out = out1;
             if (MULTI) {
@@ -611,8 +625,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             gS[i] = gL[i] = splat(T(0));
                             gC[i] = cn;
                             if (STATS) {
-                                if (v0) acc[0] += (double)fl.x() * (double)fl.x();
-                                if (v1) acc[0] += (double)fl.y() * (double)fl.y();
+                                const V2<T> f = FULL ? fl : V2<T>(v0 ? fl.x() : T(0), v1 ? fl.y() : T(0));
+                                acc[0] = fma2(f, f, acc[0]);
                             }
                         } else {
                             const V2<T> eS = Qr.S[i], eL = Qr.L[i], dmu = Qr.d[i];
@@ -648,16 +662,12 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             gL[i] = Ln;
                             gC[i] = cn;
                             if (STATS) {
-                                if (v0) {
-                                    acc[0] += (double)fl.x() * (double)fl.x();
-                                    acc[1] += (double)dS.x() * (double)dS.x();
-                                    acc[2] += (double)dL.x() * (double)dL.x();
-                                }
-                                if (v1) {
-                                    acc[0] += (double)fl.y() * (double)fl.y();
-                                    acc[1] += (double)dS.y() * (double)dS.y();
-                                    acc[2] += (double)dL.y() * (double)dL.y();
-                                }
+                                const V2<T> f = FULL ? fl : V2<T>(v0 ? fl.x() : T(0), v1 ? fl.y() : T(0));
+                                const V2<T> ds = FULL ? dS : V2<T>(v0 ? dS.x() : T(0), v1 ? dS.y() : T(0));
+                                const V2<T> dl = FULL ? dL : V2<T>(v0 ? dL.x() : T(0), v1 ? dL.y() : T(0));
+                                acc[0] = fma2(f, f, acc[0]);
+                                acc[1] = fma2(ds, ds, acc[1]);
+                                acc[2] = fma2(dl, dl, acc[2]);
                             }
                         }
                     }
@@ -737,11 +747,11 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 __syncthreads();
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
-                    double v = acc[i];
+                    double v = (double)acc[i].x() + (double)acc[i].y();
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
                     if (lane == 0) ired[warp][i] = v;
-                    acc[i] = 0.0;
+                    acc[i] = splat(T(0));
                 }
                 __syncthreads();
                 if (tid == 0)
@@ -882,8 +892,29 @@ int tma_grid(const Geom &g, int num_sms, int *zc_out) {
     return (int)best_grid;
 }
 
+// The z split of a launch choice: chunks of zc, the top `tail` planes
+// (rounded so that the chunks below are whole) in chunks of zc2; zc2 = 0 or
+// tail = 0 cuts uniformly.
+static ZSplit zsplit(const Geom &g, const StepTune &t) {
+    ZSplit s;
+    s.zc = t.zc < 1 ? 1 : (t.zc > g.nz ? g.nz : t.zc);
+    const bool two = t.zc2 > 0 && t.tail > 0 && t.zc2 < s.zc;
+    s.zc2 = two ? t.zc2 : s.zc;
+    const int below = two ? (t.tail < g.nz ? g.nz - t.tail : 0) : g.nz;
+    s.n1 = below / s.zc;
+    return s;
+}
+
 template <typename T>
-int tma_grid_for_zc(const Geom &g, int num_sms, int zc) {
+int64_t tma_items(const Geom &g, const StepTune &t) {
+    using G = TmaGeo<T>;
+    const ZSplit s = zsplit(g, t);
+    const int64_t chunks = s.n1 + (g.nz - s.n1 * s.zc + s.zc2 - 1) / s.zc2;
+    return (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY) * chunks;
+}
+
+template <typename T>
+int tma_grid_for(const Geom &g, int num_sms, const StepTune &t) {
     using G = TmaGeo<T>;
     int dummy = 0;
     if (tma_grid<T>(g, num_sms, &dummy) < 1) return -1;    // attributes + occupancy
@@ -891,21 +922,10 @@ int tma_grid_for_zc(const Geom &g, int num_sms, int zc) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 1, false, false>, G::NT,
                                                       tma_smem_bytes<T>()) != cudaSuccess || occ < 1)
         occ = 1;
-    const int64_t ntiles = (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY);
-    if (zc < 1) zc = 1;
-    if (zc > g.nz) zc = g.nz;
-    const int64_t items = ntiles * ((g.nz + zc - 1) / zc);
+    const int64_t items = tma_items<T>(g, t);
     const int64_t slots = (int64_t)occ * num_sms;
     if (items > ((int64_t)1 << 30)) return -1;
     return (int)(items < slots ? items : slots);
-}
-
-template <typename T>
-int64_t tma_items(const Geom &g, int zc) {
-    using G = TmaGeo<T>;
-    if (zc < 1) zc = 1;
-    if (zc > g.nz) zc = g.nz;
-    return (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY) * ((g.nz + zc - 1) / zc);
 }
 
 // A launch of the single-domain step; with `pdl` the launch allows
@@ -938,10 +958,12 @@ static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, F
     const bool st = partials != nullptr;
     const CoefV<T> kv = make_coefv(k);
     const DomainDesc *no_table = nullptr;
+    const ZSplit zs = zsplit(g, tune);
+    const int items = (int)tma_items<T>(g, tune);
 #define PPF_LAUNCH(ST, CO, EQ)                                                                                        \
     launch_step_ex(tune.pdl != 0, step_tma_kernel<T, ST, CO, EQ, R, false, FULL>, tune.grid, G::NT, sh, s, maps[0],   \
-                   maps[1], maps[2], g, k, kv, out, ntx, nty, tune.zc, partials, err, limit_ns, inject_stall,        \
-                   no_table, 0, 0, 0, tune.sched ? sched : nullptr)
+                   maps[1], maps[2], g, k, kv, out, ntx, nty, zs, partials, err, limit_ns, inject_stall, no_table, 0, \
+                   items, 0, tune.sched ? sched : nullptr)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -982,8 +1004,9 @@ static void launch_multi_r(const DomainDesc *table, int ndom, int items, const C
     memset(&g0, 0, sizeof g0);
     const Fields<T> o0 = {nullptr, nullptr, nullptr};
     const CoefV<T> kv = make_coefv(k);
+    const ZSplit z1 = {1, 1, 1};
 #define PPF_LAUNCH(ST, CO, EQ)                                                                                       \
-    step_tma_kernel<T, ST, CO, EQ, R, true, false><<<grid, G::NT, sh, s>>>(none, none, none, g0, k, kv, o0, 1, 1, 1, \
+    step_tma_kernel<T, ST, CO, EQ, R, true, false><<<grid, G::NT, sh, s>>>(none, none, none, g0, k, kv, o0, 1, 1, z1, \
                                                                            partials, err, limit_ns, 0, table, ndom, \
                                                                            items, parity, sched)
     if (eqA) {

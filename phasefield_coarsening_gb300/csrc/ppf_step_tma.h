@@ -26,6 +26,8 @@ struct StepTune {
     int roll;   // 3: plane body unrolled three times; 1: one copy
     int pdl;    // 1: consecutive launches overlap by programmatic dependent launch
     int sched;  // 1: CTAs take work items from a global counter; 0: round-robin
+    int zc2;    // > 0 (and < zc): the top `tail` planes are cut into chunks of zc2
+    int tail;
 };
 
 // Tensor map of one padded field (3-D: x pitch, ny+2 rows, nz+2 planes)
@@ -38,9 +40,9 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map);
 template <typename T>
 int tma_grid(const Geom &g, int num_sms, int *zc);
 
-// Grid for a given z chunk length.
+// Grid for a launch choice (occupancy x SMs, capped by its work items).
 template <typename T>
-int tma_grid_for_zc(const Geom &g, int num_sms, int zc);
+int tma_grid_for(const Geom &g, int num_sms, const StepTune &t);
 
 // One fused step.  maps = {etaS, etaL, c} of the input state; eqA selects
 // the specialisation for AS == AL (mu needs no reciprocal); `partials`
@@ -55,9 +57,9 @@ cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *
                             bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
                             int inject_stall, int *sched, cudaStream_t s);
 
-// Work items of one single-domain step with z chunk zc.
+// Work items of one single-domain step with the launch choice's z split.
 template <typename T>
-int64_t tma_items(const Geom &g, int zc);
+int64_t tma_items(const Geom &g, const StepTune &t);
 
 // Tiles of the fused step (x, y), for sizing ensemble work items.
 template <typename T>

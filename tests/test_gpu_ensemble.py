@@ -38,8 +38,11 @@ def test_ensemble_equals_independent_domains(precision, bc, sched):
             ref, rs = _single(sh, st, 37, bc, precision, pieces=(1, 36))
             for a, b in zip(got, ref):
                 assert np.array_equal(a, b), (d, sh)
+            # per-thread sums in the state's precision per work item, grouped
+            # differently by the ensemble's work items
             np.testing.assert_allclose([gs["sum_dc2"], gs["sum_detaS2"], gs["sum_detaL2"]],
-                                       [rs["sum_dc2"], rs["sum_detaS2"], rs["sum_detaL2"]], rtol=1e-12)
+                                       [rs["sum_dc2"], rs["sum_detaS2"], rs["sum_detaL2"]],
+                                       rtol=1e-12 if precision == "f64" else 1e-5)
             assert gs["steps"] == 37 and gs["mass"] == rs["mass"]
 
 

@@ -31,5 +31,10 @@ def test_slabs_equal_the_undivided_domain(precision, bc, nslabs):
     for a, b in zip(got, ref):
         assert np.array_equal(a, b)
     assert gst["cells"] == rst["cells"] and gst["nonfinite"] == 0
-    for k in ("mass", "solid", "free_energy", "sum_dc2", "sum_detaS2", "sum_detaL2"):
+    for k in ("mass", "solid", "free_energy"):
         assert abs(gst[k] - rst[k]) <= 1e-12 * abs(rst[k]) + 1e-300, k
+    # the increment sums are per-thread sums in the state's precision per
+    # work item, grouped differently by the slabs' work items
+    rel = 1e-12 if precision == "f64" else 1e-5
+    for k in ("sum_dc2", "sum_detaS2", "sum_detaL2"):
+        assert abs(gst[k] - rst[k]) <= rel * abs(rst[k]) + 1e-300, k

@@ -258,20 +258,23 @@ def test_ppf_program_matches_reference_run(name, tmp_path):
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 def test_launch_choices_are_bit_identical(precision):
-    """The z chunk, the unroll, the launch overlap and the way CTAs take work
-    items (counter or round-robin) change only who computes a cell, never the
-    arithmetic: every launch choice gives the same bits.  The last step's
-    increment sums are summed per work item in item order, so for one z
-    chunk they are the same bits whichever CTA took which item; another z
-    chunk groups the same terms differently."""
+    """The z chunk (uniform, or shorter chunks at the top of z), the unroll,
+    the launch overlap and the way CTAs take work items (counter or
+    round-robin) change only who computes a cell, never the arithmetic: every
+    launch choice gives the same bits.  The last step's increment sums are
+    summed per work item in item order, so for one z split they are the same
+    bits whichever CTA took which item; another split groups the same terms
+    differently."""
     shape = (40, 35, 70)
     st = smooth_state(shape, seed=12)
     ref, inc_of = None, {}
-    for zc, roll, pdl, sched in [(None, None, None, None), (1, 3, 1, 1), (1, 1, 0, 0), (7, 1, 0, 0), (7, 3, 1, 1),
-                                 (40, 3, 0, 1), (40, 1, 1, 0), (13, 1, 1, 0), (13, 3, 0, 1), (2, 1, 1, 1)]:
+    for zc, roll, pdl, sched, zc2, tail in [
+            (None,) * 6, (1, 3, 1, 1, 0, 0), (1, 1, 0, 0, 0, 0), (7, 1, 0, 0, 0, 0), (7, 3, 1, 1, 0, 0),
+            (40, 3, 0, 1, 0, 0), (40, 1, 1, 0, 0, 0), (13, 1, 1, 0, 0, 0), (13, 3, 0, 1, 0, 0), (2, 1, 1, 1, 0, 0),
+            (12, 3, 1, 1, 4, 10), (12, 1, 1, 0, 4, 10), (9, 1, 0, 1, 2, 31), (16, 3, 1, 1, 5, 40)]:
         with ppf.Simulation(shape, bc=1, precision=precision) as s:
             if zc is not None:
-                s.set_tune(zc, roll, pdl, sched)
+                s.set_tune(zc, roll, pdl, sched, zc2, tail)
             s.upload(*st)
             for _ in range(3):            # several launches: every launch resets the counter
                 s.step(2)
@@ -282,11 +285,12 @@ def test_launch_choices_are_bit_identical(precision):
             ref, ref_inc = out, inc
         else:
             for a, b in zip(out, ref):
-                assert np.array_equal(a, b), (zc, roll, pdl, sched)
-            np.testing.assert_allclose(inc, ref_inc, rtol=1e-13)
-            if zc in inc_of:
-                assert inc == inc_of[zc], (zc, roll, pdl, sched)
-            inc_of[zc] = inc
+                assert np.array_equal(a, b), (zc, roll, pdl, sched, zc2, tail)
+            np.testing.assert_allclose(inc, ref_inc, rtol=1e-13 if precision == "f64" else 1e-5)
+            split = (zc, zc2, tail)
+            if split in inc_of:
+                assert inc == inc_of[split], (zc, roll, pdl, sched, zc2, tail)
+            inc_of[split] = inc
 
 
 def test_autotune_keeps_state_and_picks_a_valid_choice():

@@ -501,7 +501,7 @@ def run_ensemble(args):
     # thread each, take alternate bench steps so that one's host-link copies
     # overlap the other's stepping (as in the single-domain line).
     ens2 = ppf.Ensemble(shapes, prm, bc="periodic", precision="f32")
-    ens2.set_tune(tune["zc"], tune["roll"], tune["sched"])
+    ens2.set_tune(tune["zc"], tune["roll"], tune["sched"], tune["pdl"])
     L = ppf.lib()
     pin_in = [[torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in d[:3]] for d in doms]
     pin_out = [[[torch.empty(s, dtype=torch.float64).pin_memory() for _ in range(3)] for s in shapes]

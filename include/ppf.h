@@ -190,7 +190,8 @@ typedef struct ppf_tune {
     int pdl;             /* 1 (the default): consecutive steps overlap by programmatic dependent
                             launch (the next step's CTAs are placed while this one's last CTAs
                             finish; every memory access still waits for the previous step);
-                            0: plain launches.  Ensembles ignore it. */
+                            0: plain launches.  With it, a step whose domain does not fill whole
+                            tiles runs its edge tiles in the tail of its whole-tile launch. */
     int sched;           /* 1 (the default): CTAs take work items from a global counter, so that
                             faster CTAs take more; 0: items dealt round-robin.  Both give the
                             same bits. */

@@ -472,8 +472,8 @@ class Ensemble:
         _check(lib().ppf_ensemble_get_tune(self._h, ctypes.byref(t)))
         return t.as_dict()
 
-    def set_tune(self, zc: int, roll: int = 1, sched: int = 1):
-        t = Tune(int(zc), int(roll), 0, 0, int(sched), 0, 0, 0.0)
+    def set_tune(self, zc: int, roll: int = 1, sched: int = 1, pdl: int = 1):
+        t = Tune(int(zc), int(roll), 0, int(pdl), int(sched), 0, 0, 0.0)
         _check(lib().ppf_ensemble_set_tune(self._h, ctypes.byref(t)))
 
     def autotune(self, trial_steps: int = 5) -> dict:

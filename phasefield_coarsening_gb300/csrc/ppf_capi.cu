@@ -329,8 +329,8 @@ int check_device_error(ppf_ctx *c) {
     CU(cudaMemcpyAsync(&h, c->derr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     if (h) {
-        // the error word, and the scheduler pair that an abandoned step may leave set
-        CU(cudaMemsetAsync(c->derr, 0, 6 * sizeof(int), c->stream));
+        // the error word, and the scheduler pairs that an abandoned step may leave set
+        CU(cudaMemsetAsync(c->derr, 0, 8 * sizeof(int), c->stream));
         CU(cudaStreamSynchronize(c->stream));
         return seterr(PPF_ETIMEOUT, "a device wait exceeded its limit; the state of that step is invalid");
     }
@@ -343,7 +343,7 @@ static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
     if (!c->uploaded) return seterr(PPF_ESTATE, "no state uploaded");
     if (nsteps == 0) return PPF_OK;
     const int64_t items = c->prec == PPF_F32 ? tma_items<float>(c->g, c->tune) : tma_items<double>(c->g, c->tune);
-    if (items > ((int64_t)1 << 30)) return seterr(PPF_EINVAL, "too many work items");
+    if (items > ((int64_t)1 << 29)) return seterr(PPF_EINVAL, "too many work items");
     int rc = ensure_partials(c, 3 * (int)items);
     if (rc) return rc;
     for (int64_t s = 0; s < nsteps; ++s) {

@@ -28,7 +28,7 @@ struct ppf_ctx {
     double *dres;         // device results: [0..2] increments, [3..7] observables, [8..12] particles,
                           // [16..19] mass-projection plan; the error word follows at dres + 32
     int *derr;            // device error word set by a kernel whose bounded wait ran out
-    int *dsched;          // the step's scheduler word pair (dres + 32, after the error word)
+    int *dsched;          // the step's two scheduler word pairs (dres + 32, after the error word)
     CUtensorMap maps[2][3];   // TMA maps of the fields of both buffers
     ppf::StepTune tune;        // launch choices of the fused step (grid, z chunk, unroll)
     unsigned long long wait_limit_ns;

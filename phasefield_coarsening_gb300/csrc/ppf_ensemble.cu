@@ -38,14 +38,19 @@ int err_(int code, const char *fmt, ...) {
         if (e_ != cudaSuccess) return err_(PPF_ECUDA, "%s: %s", #call, cudaGetErrorString(e_));   \
     } while (0)
 
-// per-domain sums of the per-item increment partials (deterministic order)
-__global__ void domain_sums(const DomainDesc *__restrict__ table, const double *__restrict__ partials,
+// per-domain sums of the per-item increment partials (deterministic order):
+// the domain's whole-tile items, then its edge-tile items, which follow all
+// `nwhole` whole-tile items in `partials`
+__global__ void domain_sums(const DomainDesc *__restrict__ table, const double *__restrict__ partials, int nwhole,
                             double *const *__restrict__ dres) {
     const DomainDesc &d = table[blockIdx.x];
     __shared__ double red[3][128];
     double a[3] = {0, 0, 0};
-    for (int i = threadIdx.x; i < d.nitems; i += blockDim.x)
-        for (int v = 0; v < 3; ++v) a[v] += partials[(int64_t)(d.item0 + i) * 3 + v];
+    const int n = d.nitems[1] + d.nitems[0];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int64_t r = i < d.nitems[1] ? d.item0[1] + i : (int64_t)nwhole + d.item0[0] + (i - d.nitems[1]);
+        for (int v = 0; v < 3; ++v) a[v] += partials[r * 3 + v];
+    }
     for (int v = 0; v < 3; ++v) red[v][threadIdx.x] = a[v];
     __syncthreads();
     for (int h = 64; h > 0; h >>= 1) {
@@ -67,7 +72,9 @@ struct ppf_ensemble {
     double **ddres;              // device: each domain's dres pointer
     double *partials;            // 3 doubles per work item
     int partials_cap;
-    int items, grid, zc, roll;
+    int items[2];                // work items of the edge-tile [0] and whole-tile [1] launches
+    int grid, zc, roll;
+    int pdl;                     // 1: launches overlap by programmatic dependent launch
     int sched;                   // 1: work items from a counter (domain 0's scheduler pair; the
                                  // ensemble's stream orders every domain's launches)
     int parity;                  // buffer holding the current state of every domain
@@ -85,7 +92,7 @@ static int build_table(ppf_ensemble *e) {
     if (e->prec == PPF_F32) step_tile<float>(&tx, &ty);
     else step_tile<double>(&tx, &ty);
     std::vector<DomainDesc> h((size_t)e->n);
-    int64_t item0 = 0;
+    int64_t item0s[2] = {0, 0};
     for (int k = 0; k < e->n; ++k) {
         ppf_ctx *c = e->dom[(size_t)e->order[(size_t)k]];
         DomainDesc &t = h[(size_t)k];
@@ -98,22 +105,29 @@ static int build_table(ppf_ensemble *e) {
         t.g = c->g;
         t.ntx = (c->nx + tx - 1) / tx;
         t.nty = (c->ny + ty - 1) / ty;
+        t.nfx = c->nx / tx;
+        t.nfy = c->ny / ty;
         t.zc = e->zc < c->nz ? e->zc : c->nz;
         t.nc = (c->nz + t.zc - 1) / t.zc;
-        t.item0 = (int)item0;
-        t.nitems = t.ntx * t.nty * t.nc;
-        item0 += t.nitems;
+        t.nitems[1] = t.nfx * t.nfy * t.nc;
+        t.nitems[0] = (t.ntx * t.nty - t.nfx * t.nfy) * t.nc;
+        for (int q = 0; q < 2; ++q) {
+            t.item0[q] = (int)item0s[q];
+            item0s[q] += t.nitems[q];
+        }
     }
-    if (item0 > ((int64_t)1 << 30)) return err_(PPF_EINVAL, "ensemble has too many work items");
-    e->items = (int)item0;
+    if (item0s[0] + item0s[1] > ((int64_t)1 << 29)) return err_(PPF_EINVAL, "ensemble has too many work items");
+    e->items[0] = (int)item0s[0];
+    e->items[1] = (int)item0s[1];
+    const int64_t item0 = item0s[0] + item0s[1];
     e->grid = e->prec == PPF_F32 ? tma_grid_items<float>(item0, e->num_sms) : tma_grid_items<double>(item0, e->num_sms);
     if (e->grid < 1) return err_(PPF_ECUDA, "no launch shape for the ensemble");
     ECU(cudaMemcpyAsync(e->dtable, h.data(), h.size() * sizeof(DomainDesc), cudaMemcpyHostToDevice, e->stream));
-    if (3 * e->items > e->partials_cap) {
+    if (3 * item0 > e->partials_cap) {
         if (e->partials) cudaFree(e->partials);
         e->partials = nullptr;
-        ECU(cudaMalloc(&e->partials, (size_t)3 * e->items * sizeof(double)));
-        e->partials_cap = 3 * e->items;
+        ECU(cudaMalloc(&e->partials, (size_t)3 * item0 * sizeof(double)));
+        e->partials_cap = (int)(3 * item0);
     }
     ECU(cudaStreamSynchronize(e->stream));
     if (e->graph_ok) cudaGraphExecDestroy(e->graph);
@@ -128,11 +142,13 @@ static int launch_one(ppf_ensemble *e, bool stats) {
     cudaError_t r;
     if (e->prec == PPF_F32)
         r = launch_step_multi<float>(e->dtable, e->n, e->items, c0->kf, false, e->eqA, e->parity,
-                                     stats ? e->partials : nullptr, e->grid, e->roll, c0->derr, c0->wait_limit_ns,
+                                     stats ? e->partials : nullptr, e->grid, e->roll, e->pdl != 0, c0->derr,
+                                     c0->wait_limit_ns,
                                      e->sched ? c0->dsched : nullptr, e->stream);
     else
         r = launch_step_multi<double>(e->dtable, e->n, e->items, c0->kd, false, e->eqA, e->parity,
-                                      stats ? e->partials : nullptr, e->grid, e->roll, c0->derr, c0->wait_limit_ns,
+                                      stats ? e->partials : nullptr, e->grid, e->roll, e->pdl != 0, c0->derr,
+                                      c0->wait_limit_ns,
                                       e->sched ? c0->dsched : nullptr, e->stream);
     if (r != cudaSuccess) return err_(PPF_ECUDA, "ensemble step launch: %s", cudaGetErrorString(r));
     e->parity ^= 1;
@@ -174,6 +190,12 @@ extern "C" int ppf_ensemble_destroy(ppf_ensemble *e) {
 extern "C" int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, int bc, int precision,
                                    ppf_ensemble **out) {
     if (!out || !dims || n < 1 || n > 4096) return err_(PPF_EINVAL, "ensemble: bad arguments");
+    for (int d = 0; d < n; ++d) {
+        // the ensemble step addresses each domain with 32-bit element offsets
+        const int64_t nz = dims[3 * d], ny = dims[3 * d + 1], nx = dims[3 * d + 2];
+        if (nz > 0 && ny > 0 && nx > 0 && (nz + 2) * (ny + 2) * (nx + 16) > ((int64_t)1 << 32))
+            return err_(PPF_EINVAL, "ensemble: domain %d holds 2^32 elements or more per field", d);
+    }
     *out = nullptr;
     ppf_ensemble *e = new (std::nothrow) ppf_ensemble();
     if (!e) return err_(PPF_ENOMEM, "host allocation failed");
@@ -183,6 +205,7 @@ extern "C" int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, 
     e->zc = 32;
     e->roll = 1;
     e->sched = 1;
+    e->pdl = 1;
     int rc = PPF_OK;
     for (int d = 0; d < n && rc == PPF_OK; ++d) {
         ppf_ctx *c = nullptr;
@@ -288,7 +311,7 @@ static int run(ppf_ensemble *e, int64_t nsteps) {
     }
     for (; left > 0 && rc == PPF_OK; --left) rc = launch_one(e, left == 1);
     if (rc) return rc;
-    domain_sums<<<e->n, 128, 0, e->stream>>>(e->dtable, e->partials, e->ddres);
+    domain_sums<<<e->n, 128, 0, e->stream>>>(e->dtable, e->partials, e->items[1], e->ddres);
     ECU(cudaGetLastError());
     for (ppf_ctx *x : e->dom) {
         x->cur_eta = x->cur_c = e->parity;
@@ -316,7 +339,7 @@ extern "C" int ppf_ensemble_get_tune(const ppf_ensemble *e, ppf_tune *t) {
     t->zc = e->zc;
     t->roll = e->roll;
     t->grid = e->grid;
-    t->pdl = 0;
+    t->pdl = e->pdl;
     t->sched = e->sched;
     t->zc2 = t->tail = 0;
     t->us_per_step = 0;
@@ -328,10 +351,12 @@ extern "C" int ppf_ensemble_set_tune(ppf_ensemble *e, const ppf_tune *t) {
     if (t->roll != 1 && t->roll != 3) return err_(PPF_EINVAL, "roll must be 1 or 3");
     if (t->zc < 1) return err_(PPF_EINVAL, "zc must be >= 1");
     if (t->sched != 0 && t->sched != 1) return err_(PPF_EINVAL, "sched must be 0 or 1");
+    if (t->pdl != 0 && t->pdl != 1) return err_(PPF_EINVAL, "pdl must be 0 or 1");
     ECU(cudaStreamSynchronize(e->stream));
     e->zc = t->zc;
     e->roll = t->roll;
     e->sched = t->sched;
+    e->pdl = t->pdl;
     return build_table(e);
 }
 
@@ -345,19 +370,21 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
     for (ppf_ctx *x : e->dom)
         if ((rc = do_unpack(x)) != PPF_OK) return rc;
     const int zcs[] = {4, 8, 12, 16, 24, 32, 48, 64, 128};
-    const int keep_zc = e->zc, keep_roll = e->roll, keep_sched = e->sched;
+    const int keep_zc = e->zc, keep_roll = e->roll, keep_sched = e->sched, keep_pdl = e->pdl;
     const int64_t keep_steps = e->steps;
-    int best_zc = keep_zc, best_roll = keep_roll, best_sched = keep_sched;
+    int best_zc = keep_zc, best_roll = keep_roll, best_sched = keep_sched, best_pdl = keep_pdl;
     float best_ms = -1.0f;
     cudaEvent_t t0, t1;
     ECU(cudaEventCreate(&t0));
     ECU(cudaEventCreate(&t1));
+    for (int pdl = 1; pdl >= 0 && rc == PPF_OK; --pdl)
     for (int sd = 1; sd >= 0 && rc == PPF_OK; --sd)
     for (int r = 0; r < 2 && rc == PPF_OK; ++r)
         for (int zc : zcs) {
             e->zc = zc;
             e->roll = r == 0 ? 1 : 3;
             e->sched = sd;
+            e->pdl = pdl;
             if ((rc = build_table(e)) != PPF_OK) break;
             for (int s = 0; s < 2 && rc == PPF_OK; ++s) rc = launch_one(e, false);     // warm-up
             if (rc) break;
@@ -368,13 +395,20 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
             if ((rc = check_device_error(e->dom[0])) != PPF_OK) break;
             float ms = 0;
             cudaEventElapsedTime(&ms, t0, t1);
-            if (best_ms < 0 || ms < best_ms) { best_ms = ms; best_zc = e->zc; best_roll = e->roll; best_sched = e->sched; }
+            if (best_ms < 0 || ms < best_ms) {
+                best_ms = ms;
+                best_zc = e->zc;
+                best_roll = e->roll;
+                best_sched = e->sched;
+                best_pdl = e->pdl;
+            }
         }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     e->zc = rc == PPF_OK ? best_zc : keep_zc;
     e->roll = rc == PPF_OK ? best_roll : keep_roll;
     e->sched = rc == PPF_OK ? best_sched : keep_sched;
+    e->pdl = rc == PPF_OK ? best_pdl : keep_pdl;
     int rc2 = build_table(e);
     for (ppf_ctx *x : e->dom)
         if (rc2 == PPF_OK) {
@@ -391,7 +425,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
         best->zc = e->zc;
         best->roll = e->roll;
         best->grid = e->grid;
-        best->pdl = 0;
+        best->pdl = e->pdl;
         best->sched = e->sched;
         best->zc2 = best->tail = 0;
         best->us_per_step = best_ms * 1000.0 / trial_steps;

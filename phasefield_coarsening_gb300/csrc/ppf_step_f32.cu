@@ -1,13 +1,11 @@
-// ppf_step_f32.cu -- the FP32 instantiations of the fused step (ppf_step_tma.cuh).
+// ppf_step_f32.cu -- the FP32 single-domain instantiations of the fused step
+// (ppf_step_tma.cuh); the ensemble ones are in ppf_step_f32_ens.cu, so that
+// the two sets of kernels compile in parallel.
 #include "ppf_step_tma.cuh"
 
 namespace ppf {
 
 template void step_tile<float>(int *, int *);
-template int tma_grid_items<float>(int64_t, int);
-template cudaError_t launch_step_multi<float>(const DomainDesc *, int, int, const Coef<float> &, bool, bool, int,
-                                            double *, int, int, int *, unsigned long long, int *,
-                                            cudaStream_t);
 template int make_field_map<float>(const Geom &, const float *, CUtensorMap *);
 template int tma_grid<float>(const Geom &, int, int *);
 template int tma_grid_for<float>(const Geom &, int, const StepTune &);

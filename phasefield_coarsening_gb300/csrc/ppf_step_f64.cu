@@ -1,13 +1,11 @@
-// ppf_step_f64.cu -- the FP64 instantiations of the fused step (ppf_step_tma.cuh).
+// ppf_step_f64.cu -- the FP64 single-domain instantiations of the fused step
+// (ppf_step_tma.cuh); the ensemble ones are in ppf_step_f64_ens.cu, so that
+// the two sets of kernels compile in parallel.
 #include "ppf_step_tma.cuh"
 
 namespace ppf {
 
 template void step_tile<double>(int *, int *);
-template int tma_grid_items<double>(int64_t, int);
-template cudaError_t launch_step_multi<double>(const DomainDesc *, int, int, const Coef<double> &, bool, bool, int,
-                                            double *, int, int, int *, unsigned long long, int *,
-                                            cudaStream_t);
 template int make_field_map<double>(const Geom &, const double *, CUtensorMap *);
 template int tma_grid<double>(const Geom &, int, int *);
 template int tma_grid_for<double>(const Geom &, int, const StepTune &);

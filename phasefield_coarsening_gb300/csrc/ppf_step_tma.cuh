@@ -315,10 +315,52 @@ struct PlaneRegs {
     V2<T> S[H], L[H], mu[H], M[H], c[H], d[H];
 };
 
-// A work item: one tile column segment of one domain.
+// A work item: one tile column segment of one domain (tile bx, by; interior
+// planes z0 .. z1-1).
 struct Item {
-    int dom, tile, z0, z1;
+    int dom, bx, by, z0, z1;
 };
+
+// The tiles of one launch.  A step is run as up to two launches over
+// disjoint tile sets: the whole tiles (SET_WHOLE: the nfx x nfy rectangle
+// of tiles inside the domain, whose plane body needs no per-cell "inside"
+// test) and the edge tiles (SET_EDGE: the column of partial tiles at high x
+// when nx is not a multiple of the tile width, then the row of partial
+// tiles at high y), or, for a domain whose fields exceed 2^32 elements, one
+// launch over every tile with 64-bit offsets (SET_ALL).
+enum { SET_ALL = 0, SET_EDGE = 1, SET_WHOLE = 2 };
+
+struct Tiles {
+    int ntx, nty;   // tiles in x and y
+    int nfx, nfy;   // whole tiles in x and y
+};
+
+__host__ __device__ inline int tiles_in_set(const Tiles &t, int set) {
+    return set == SET_ALL ? t.ntx * t.nty : set == SET_WHOLE ? t.nfx * t.nfy : t.ntx * t.nty - t.nfx * t.nfy;
+}
+
+// tile k of the set
+template <int SET>
+__device__ __forceinline__ void tile_of(int k, const Tiles &t, int &bx, int &by) {
+    if (SET == SET_ALL) {
+        by = k / t.ntx;
+        bx = k - by * t.ntx;
+    } else if (SET == SET_WHOLE) {
+        by = k / t.nfx;
+        bx = k - by * t.nfx;
+    } else {
+        if (t.nfx < t.ntx) {           // the high-x column of partial tiles
+            if (k < t.nty) {
+                bx = t.nfx;
+                by = k;
+                return;
+            }
+            k -= t.nty;
+        }
+        bx = k;                        // the high-y row of partial tiles
+        by = t.nfy;
+    }
+}
 
 // How a single domain's z range is cut into work-item chunks: n1 chunks of
 // zc planes, then chunks of zc2 planes up to nz (the last one may be
@@ -328,47 +370,52 @@ struct ZSplit {
     int zc, zc2, n1;
 };
 
-// Work item `item` of the launch.  Single domain: (z chunk, tile) in
-// chunk-major order.  Ensemble (MULTI): the items of each domain are
-// contiguous, chunk-major within the domain.
-template <bool MULTI>
-__device__ __forceinline__ Item item_at(int item, int ntiles, const ZSplit &zs, int nz, const DomainDesc *table,
+// Work item `item` of the launch.  Single domain: (z chunk, tile of the
+// set) in chunk-major order.  Ensemble (MULTI): the items of each domain are
+// contiguous, chunk-major within the domain (the set's item range of each
+// domain in the table; a domain may have none).
+template <bool MULTI, int SET>
+__device__ __forceinline__ Item item_at(int item, const Tiles &t1, const ZSplit &zs, int nz, const DomainDesc *table,
                                         int ndom) {
     Item it;
     if (!MULTI) {
-        const int c = item / ntiles;
+        const int nt = tiles_in_set(t1, SET);
+        const int c = item / nt;
         it.dom = 0;
-        it.tile = item - c * ntiles;
+        tile_of<SET>(item - c * nt, t1, it.bx, it.by);
         it.z0 = c < zs.n1 ? c * zs.zc : zs.n1 * zs.zc + (c - zs.n1) * zs.zc2;
         it.z1 = min(nz, it.z0 + (c < zs.n1 ? zs.zc : zs.zc2));
         return it;
     }
+    const int s = SET == SET_WHOLE ? 1 : 0;
     int lo = 0, hi = ndom - 1;                 // last domain with item0 <= item
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (table[mid].item0 <= item) lo = mid;
+        if (table[mid].item0[s] <= item) lo = mid;
         else hi = mid - 1;
     }
     const DomainDesc &d = table[lo];
-    const int li = item - d.item0, nt = d.ntx * d.nty;
+    const Tiles td = {d.ntx, d.nty, d.nfx, d.nfy};
+    const int nt = tiles_in_set(td, SET);
+    const int li = item - d.item0[s];
     const int c = li / nt;
     it.dom = lo;
-    it.tile = li - c * nt;
+    tile_of<SET>(li - c * nt, td, it.bx, it.by);
     it.z0 = c * d.zc;
     it.z1 = min(d.g.nz, it.z0 + d.zc);
     return it;
 }
 
-// FULL: every tile of the launch lies inside the domain (nx, ny multiples of
-// the tile), so no cell needs the per-cell "inside the domain" test.
-template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL, bool MULTI, bool FULL>
+// SET: the launch's tiles (SET_WHOLE: no per-cell "inside the domain" test;
+// SET_EDGE: with it; SET_ALL: with it and 64-bit element offsets, for fields
+// of more than 2^32 elements; the other sets use 32-bit offsets).
+template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL, bool MULTI, int SET>
 __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
                     const __grid_constant__ CUtensorMap mapC, Geom g1, Coef<T> k, CoefV<T> kv, Fields<T> out1,
-                    int ntx1, int nty1,
-                    ZSplit zs1, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
+                    Tiles t1, ZSplit zs1, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
                     int inject_stall, const DomainDesc *__restrict__ table, int ndom, int mitems, int parity,
-                    int *__restrict__ sched) {
+                    int *__restrict__ sched, int second) {
     using G = TmaGeo<T>;
     constexpr int TX = G::TX, TY = G::TY, S = G::S, XH = G::XH, BX = G::BX, CY = G::CY;
     extern __shared__ __align__(128) unsigned char smem_dyn[];
@@ -378,20 +425,26 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const uint32_t pad = (128u - (smem_u32(smem_dyn) & 127u)) & 127u;
     TmaSmem<T> &sm = *reinterpret_cast<TmaSmem<T> *>(smem_dyn + pad);
 
-    // programmatic dependent launch: let the next step's grid be scheduled
-    // now (its CTAs take SM slots as this grid's CTAs leave), and wait for
-    // the previous grid -- which reads what this one writes and writes what
-    // it reads -- to complete before touching global memory.  Both are no-ops
-    // when the launch does not allow the overlap.
+    // Programmatic dependent launch (no-ops when the launch does not allow
+    // the overlap).  A step is one launch, or two over disjoint tile sets
+    // that read the same input and write disjoint cells.  The first launch
+    // of a step waits for the previous grid -- the previous step, which wrote
+    // what it reads -- to complete, and then lets the next grid be scheduled
+    // (its CTAs take SM slots as this grid's CTAs leave).  The second launch
+    // of a step (`second`) depends on nothing of the first: its CTAs start
+    // in the first launch's tail, since that launch let it be scheduled only
+    // after the previous step had completed, and they wait for the first
+    // launch to complete only before they exit, so that this grid's end
+    // also ends the step.
+    if (!second) asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = (warp % G::WX) * 32 + lane;        // own column in the tile
     const int ty0 = (warp / G::WX) * CY;              // first own row in the tile
-    const int ntiles1 = ntx1 * nty1;
     const int nitems = mitems;
     const int ob = (ty0 + 1) * BX + tx + XH;          // shared offset of the first own cell
-    static_assert(!(MULTI && FULL), "ensembles take the general path");
+    static_assert(!(MULTI && SET == SET_ALL), "ensemble domains hold fewer than 2^32 elements per field");
+    constexpr bool FULL = SET == SET_WHOLE;
     // the pair of cells of the one-cell ring around the tile that this thread
     // evaluates: the last RING/2 threads (warp 0 also feeds the TMA ring), each
     // a cell of the top row with the one below it in the bottom row, or a cell
@@ -467,15 +520,13 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
         Item p_it;
         auto p_set = [&]() {
             if (p_item < nitems) {
-                p_it = item_at<MULTI>(p_item, ntiles1, zs1, g1.nz, table, ndom);
+                p_it = item_at<MULTI, SET>(p_item, t1, zs1, g1.nz, table, ndom);
                 p_pz = p_it.z0 - 1;
                 // the item's box corner: storage x of the box start (16-byte
                 // aligned) and storage y of interior row y0-1
-                const int ntx = MULTI ? table[p_it.dom].ntx : ntx1;
                 const int xoff = MULTI ? table[p_it.dom].g.xoff : g1.xoff;
-                const int by = p_it.tile / ntx, bx = p_it.tile - by * ntx;
-                p_xs = bx * TX + xoff - XH;
-                p_ys = by * TY;
+                p_xs = p_it.bx * TX + xoff - XH;
+                p_ys = p_it.by * TY;
                 if (MULTI) {
                     p_mS = &table[p_it.dom].maps[parity][0];
                     p_mL = &table[p_it.dom].maps[parity][1];
@@ -524,7 +575,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
         for (int seq = 0; !dead; ++seq) {
             const int item = s_next[seq & 1];
             if (item >= nitems) break;
-            const Item it = item_at<MULTI>(item, ntiles1, zs1, g1.nz, table, ndom);
+            const Item it = item_at<MULTI, SET>(item, t1, zs1, g1.nz, table, ndom);
             const Geom g = MULTI ? table[it.dom].g : g1;
             Fields<T> out = out1;
             if (MULTI) {
@@ -532,9 +583,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 out.eL = (T *)table[it.dom].fld[1 - parity][1];
                 out.c = (T *)table[it.dom].fld[1 - parity][2];
             }
-            const int ntx = MULTI ? table[it.dom].ntx : ntx1;
-            const int bx = it.tile % ntx, by = it.tile / ntx;
-            const int x0 = bx * TX, y0 = by * TY, z0 = it.z0, z1 = it.z1;
+            const int x0 = it.bx * TX, y0 = it.by * TY, z0 = it.z0, z1 = it.z1;
             const int X = x0 + tx;
             // per own row j: inside the domain (bit j of vmask)
             unsigned vmask = 0;
@@ -584,9 +633,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 if (q >= z0) {
                     const T *nS = sm.raw[st_prev][0], *nL = sm.raw[st_prev][1];
                     const T *nmu = sm.mm[mb_prev][0], *nM = sm.mm[mb_prev][1];
-                    // FULL launches address the state with 32-bit element offsets (the
-                    // host takes that variant only when every offset fits)
-                    using Off = typename std::conditional<FULL, uint32_t, int64_t>::type;
+                    // 32-bit element offsets unless the fields exceed 2^32 elements
+                    using Off = typename std::conditional<SET == SET_ALL, int64_t, uint32_t>::type;
                     const Off base = (Off)col + (Off)(q + 1) * (Off)g.PS;
                     // the new values of the plane's own cells, kept for the face ghosts below
                     V2<T> gS[H], gL[H], gC[H];
@@ -594,10 +642,8 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     for (int i = 0; i < H; ++i) {
                         const int j0 = i, j1 = i + H;                       // the pair's cells
                         const bool v0 = FULL || (vmask & (1u << j0)), v1 = FULL || (vmask & (1u << j1));
-                        if (!FULL && !(v0 || v1)) {
-                            gS[i] = gL[i] = gC[i] = splat(T(0));   // outside: never feeds a ghost
-                            continue;
-                        }
+                        // (a pair outside the domain is computed from whatever the
+                        // box holds there; nothing of it is stored or summed)
                         const int o0 = ob + j0 * BX, o1 = ob + j1 * BX;
                         const V2<T> mu = Qr.mu[i], M = Qr.M[i], c = Qr.c[i];
                         // y neighbours: pair i-1 / i+1, or a shared row at the column ends
@@ -618,10 +664,15 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                         fl = fma2(Mxp + M, muxp - mu, fl);
                         fl = fma2(Mxm + M, muxm - mu, fl);
                         const V2<T> cn = c + fl;
-                        const Off a0 = base + (Off)j0 * (Off)g.P, a1 = base + (Off)j1 * (Off)g.P;
+                        // a cell outside the domain stores to the first element of its
+                        // plane (column 0 of ghost row -1: padding that nothing reads),
+                        // so that the stores need no predicate
+                        const Off sink = base - (Off)col;
+                        const Off a0 = v0 ? base + (Off)j0 * (Off)g.P : sink;
+                        const Off a1 = v1 ? base + (Off)j1 * (Off)g.P : sink;
                         if (C_ONLY) {
-                            if (v0) out.c[a0] = cn.x();
-                            if (v1) out.c[a1] = cn.y();
+                            out.c[a0] = cn.x();
+                            out.c[a1] = cn.y();
                             gS[i] = gL[i] = splat(T(0));
                             gC[i] = cn;
                             if (STATS) {
@@ -648,16 +699,12 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                             const V2<T> dS = fma2(mt * eS, fma2(tg, L2, S2 - one), fma2(nkt, lapS, eL * dmu));
                             const V2<T> dL = fma2(mt * eL, fma2(tg, S2, L2 - one), fma2(nkt, lapL, V2<T>(kv.zero) - eS * dmu));
                             const V2<T> Sn = eS + dS, Ln = eL + dL;
-                            if (v0) {
-                                out.eS[a0] = Sn.x();
-                                out.eL[a0] = Ln.x();
-                                out.c[a0] = cn.x();
-                            }
-                            if (v1) {
-                                out.eS[a1] = Sn.y();
-                                out.eL[a1] = Ln.y();
-                                out.c[a1] = cn.y();
-                            }
+                            out.eS[a0] = Sn.x();
+                            out.eL[a0] = Ln.x();
+                            out.c[a0] = cn.x();
+                            out.eS[a1] = Sn.y();
+                            out.eL[a1] = Ln.y();
+                            out.c[a1] = cn.y();
                             gS[i] = Sn;
                             gL[i] = Ln;
                             gC[i] = cn;
@@ -773,9 +820,9 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     atomicExch(&sched[1], 0);
                 }
             }
-            return;
         }
     }
+    if (second) asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 // ------------------------------------------------------------------ host --
@@ -809,34 +856,39 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map) {
     return r == CUDA_SUCCESS ? 0 : -3;
 }
 
-template <typename T, bool ST, bool CO, bool EQ, int R>
+template <typename T, bool ST, bool CO, bool EQ, int R, bool M>
 static cudaError_t set_attr1() {
+    // (single-domain and ensemble variants are set up, and compiled, in
+    // separate translation units)
     const int sh = (int)tma_smem_bytes<T>();
-    cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, sh);
-    if (e) return e;
-    e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, sh);
-    if (e) return e;
-    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, true, false>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, sh);
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e;
+    if (M) {
+        if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, true, SET_EDGE>, a, sh))) return e;
+        return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, true, SET_WHOLE>, a, sh);
+    }
+    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, SET_ALL>, a, sh)) ||
+        (e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, SET_EDGE>, a, sh)))
+        return e;
+    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, SET_WHOLE>, a, sh);
 }
 
-template <typename T, int R>
+template <typename T, int R, bool M>
 static cudaError_t set_attrs_r() {
     cudaError_t e;
-    if ((e = set_attr1<T, false, false, false, R>()) || (e = set_attr1<T, true, false, false, R>()) ||
-        (e = set_attr1<T, false, true, false, R>()) || (e = set_attr1<T, true, true, false, R>()) ||
-        (e = set_attr1<T, false, false, true, R>()) || (e = set_attr1<T, true, false, true, R>()) ||
-        (e = set_attr1<T, false, true, true, R>()) || (e = set_attr1<T, true, true, true, R>()))
+    if ((e = set_attr1<T, false, false, false, R, M>()) || (e = set_attr1<T, true, false, false, R, M>()) ||
+        (e = set_attr1<T, false, true, false, R, M>()) || (e = set_attr1<T, true, true, false, R, M>()) ||
+        (e = set_attr1<T, false, false, true, R, M>()) || (e = set_attr1<T, true, false, true, R, M>()) ||
+        (e = set_attr1<T, false, true, true, R, M>()) || (e = set_attr1<T, true, true, true, R, M>()))
         return e;
     return cudaSuccess;
 }
 
-template <typename T>
+// M: the ensemble variants, else the single-domain ones
+template <typename T, bool M>
 static cudaError_t set_attrs() {
-    cudaError_t e = set_attrs_r<T, 1>();
-    return e ? e : set_attrs_r<T, 3>();
+    cudaError_t e = set_attrs_r<T, 1, M>();
+    return e ? e : set_attrs_r<T, 3, M>();
 }
 
 // Launch shape.  Work items are (z chunk, tile) pairs dealt round-robin to
@@ -853,9 +905,9 @@ int tma_grid(const Geom &g, int num_sms, int *zc_out) {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
     int &occ = occ_of[dev];
     if (!occ) {
-        if (set_attrs<T>() != cudaSuccess) return -1;
+        if (set_attrs<T, false>() != cudaSuccess) return -1;
         int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 1, false, false>, G::NT,
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 1, false, SET_WHOLE>, G::NT,
                                                           tma_smem_bytes<T>()) != cudaSuccess || o < 1)
             o = 1;
         occ = o;
@@ -919,7 +971,7 @@ int tma_grid_for(const Geom &g, int num_sms, const StepTune &t) {
     int dummy = 0;
     if (tma_grid<T>(g, num_sms, &dummy) < 1) return -1;    // attributes + occupancy
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 1, false, false>, G::NT,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 1, false, SET_WHOLE>, G::NT,
                                                       tma_smem_bytes<T>()) != cudaSuccess || occ < 1)
         occ = 1;
     const int64_t items = tma_items<T>(g, t);
@@ -948,22 +1000,34 @@ static void launch_step_ex(bool pdl, void (*kern)(KArgs...), int grid, int block
     (void)cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
-template <typename T, int R, bool FULL>
-static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only, bool eqA,
-                     double *partials, const StepTune &tune, int *err, unsigned long long limit_ns, int inject_stall,
-                     int *sched, cudaStream_t s) {
+template <typename T>
+Tiles tiles_of(const Geom &g) {
     using G = TmaGeo<T>;
-    const int ntx = (g.nx + G::TX - 1) / G::TX, nty = (g.ny + G::TY - 1) / G::TY;
+    Tiles t;
+    t.ntx = (g.nx + G::TX - 1) / G::TX;
+    t.nty = (g.ny + G::TY - 1) / G::TY;
+    t.nfx = g.nx / G::TX;
+    t.nfy = g.ny / G::TY;
+    return t;
+}
+
+// One launch of the single-domain step over the items of one tile set.
+template <typename T, int R, int SET>
+static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only, bool eqA,
+                     double *partials, const StepTune &tune, int items, int *err, unsigned long long limit_ns,
+                     int inject_stall, int *sched, int second, cudaStream_t s) {
+    using G = TmaGeo<T>;
     const size_t sh = tma_smem_bytes<T>();
     const bool st = partials != nullptr;
     const CoefV<T> kv = make_coefv(k);
     const DomainDesc *no_table = nullptr;
     const ZSplit zs = zsplit(g, tune);
-    const int items = (int)tma_items<T>(g, tune);
+    const Tiles t = tiles_of<T>(g);
+    const int grid = items < tune.grid ? items : tune.grid;
 #define PPF_LAUNCH(ST, CO, EQ)                                                                                        \
-    launch_step_ex(tune.pdl != 0, step_tma_kernel<T, ST, CO, EQ, R, false, FULL>, tune.grid, G::NT, sh, s, maps[0],   \
-                   maps[1], maps[2], g, k, kv, out, ntx, nty, zs, partials, err, limit_ns, inject_stall, no_table, 0, \
-                   items, 0, tune.sched ? sched : nullptr)
+    launch_step_ex(tune.pdl != 0, step_tma_kernel<T, ST, CO, EQ, R, false, SET>, grid, G::NT, sh, s, maps[0],         \
+                   maps[1], maps[2], g, k, kv, out, t, zs, partials, err, limit_ns, inject_stall, no_table, 0, items,   \
+                   0, tune.sched ? sched : nullptr, second)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -974,27 +1038,43 @@ static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, F
 #undef PPF_LAUNCH
 }
 
+template <typename T, int R>
+static void launch_sets(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
+                        bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
+                        int inject_stall, int *sched, cudaStream_t s) {
+    const Tiles t = tiles_of<T>(g);
+    const int64_t chunks = tma_items<T>(g, tune) / ((int64_t)t.ntx * t.nty);
+    if (g.total > ((int64_t)1 << 32)) {        // 64-bit offsets: one launch over every tile
+        launch_r<T, R, SET_ALL>(g, k, maps, out, c_only, eqA, partials, tune, (int)(chunks * t.ntx * t.nty), err,
+                                limit_ns, inject_stall, sched, 0, s);
+        return;
+    }
+    // the whole tiles, then the edge tiles (their increment sums follow the
+    // whole tiles' in `partials`; their own scheduler pair, since the two
+    // launches overlap)
+    const int nw = (int)(chunks * tiles_in_set(t, SET_WHOLE)), ne = (int)(chunks * tiles_in_set(t, SET_EDGE));
+    if (nw > 0)
+        launch_r<T, R, SET_WHOLE>(g, k, maps, out, c_only, eqA, partials, tune, nw, err, limit_ns, inject_stall, sched,
+                                  0, s);
+    if (ne > 0)
+        launch_r<T, R, SET_EDGE>(g, k, maps, out, c_only, eqA, partials ? partials + 3 * (int64_t)nw : nullptr, tune,
+                                 ne, err, limit_ns, nw > 0 ? 0 : inject_stall, sched ? sched + 2 : nullptr,
+                                 nw > 0 ? 1 : 0, s);
+}
+
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
                             bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
                             int inject_stall, int *sched, cudaStream_t s) {
-    using G = TmaGeo<T>;
-    // FULL: every tile inside the domain, and every element offset below 2^32
-    const bool full = g.nx % G::TX == 0 && g.ny % G::TY == 0 && g.total <= ((int64_t)1 << 32);
-    if (tune.roll == 1) {
-        if (full) launch_r<T, 1, true>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
-        else launch_r<T, 1, false>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
-    } else {
-        if (full) launch_r<T, 3, true>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
-        else launch_r<T, 3, false>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
-    }
+    if (tune.roll == 1) launch_sets<T, 1>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
+    else launch_sets<T, 3>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
     return cudaGetLastError();
 }
 
-template <typename T, int R>
+template <typename T, int R, int SET>
 static void launch_multi_r(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
                            int parity, double *partials, int grid, int *err, unsigned long long limit_ns,
-                           int *sched, cudaStream_t s) {
+                           int *sched, bool pdl, int second, cudaStream_t s) {
     using G = TmaGeo<T>;
     const size_t sh = tma_smem_bytes<T>();
     const bool st = partials != nullptr;
@@ -1005,10 +1085,11 @@ static void launch_multi_r(const DomainDesc *table, int ndom, int items, const C
     const Fields<T> o0 = {nullptr, nullptr, nullptr};
     const CoefV<T> kv = make_coefv(k);
     const ZSplit z1 = {1, 1, 1};
+    const Tiles t0 = {1, 1, 1, 1};
+    if (items < grid) grid = items;
 #define PPF_LAUNCH(ST, CO, EQ)                                                                                       \
-    step_tma_kernel<T, ST, CO, EQ, R, true, false><<<grid, G::NT, sh, s>>>(none, none, none, g0, k, kv, o0, 1, 1, z1, \
-                                                                           partials, err, limit_ns, 0, table, ndom, \
-                                                                           items, parity, sched)
+    launch_step_ex(pdl, step_tma_kernel<T, ST, CO, EQ, R, true, SET>, grid, G::NT, sh, s, none, none, none, g0, k, kv, \
+                   o0, t0, z1, partials, err, limit_ns, 0, table, ndom, items, parity, sched, second)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -1020,11 +1101,23 @@ static void launch_multi_r(const DomainDesc *table, int ndom, int items, const C
 }
 
 template <typename T>
-cudaError_t launch_step_multi(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
-                              int parity, double *partials, int grid, int roll, int *err,
+cudaError_t launch_step_multi(const DomainDesc *table, int ndom, const int *items, const Coef<T> &k, bool c_only,
+                              bool eqA, int parity, double *partials, int grid, int roll, bool pdl, int *err,
                               unsigned long long limit_ns, int *sched, cudaStream_t s) {
-    if (roll == 1) launch_multi_r<T, 1>(table, ndom, items, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, s);
-    else launch_multi_r<T, 3>(table, ndom, items, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, s);
+    // the whole tiles of every domain, then the edge tiles (their increment
+    // sums follow the whole tiles' in `partials`; their own scheduler pair,
+    // since the two launches overlap)
+    const int nw = items[1], ne = items[0];
+    double *pe = partials ? partials + 3 * (int64_t)nw : nullptr;
+    int *se = sched ? sched + 2 : nullptr;
+    const int sec = nw > 0 ? 1 : 0;
+    if (roll == 1) {
+        if (nw > 0) launch_multi_r<T, 1, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
+        if (ne > 0) launch_multi_r<T, 1, SET_EDGE>(table, ndom, ne, k, c_only, eqA, parity, pe, grid, err, limit_ns, se, pdl, sec, s);
+    } else {
+        if (nw > 0) launch_multi_r<T, 3, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
+        if (ne > 0) launch_multi_r<T, 3, SET_EDGE>(table, ndom, ne, k, c_only, eqA, parity, pe, grid, err, limit_ns, se, pdl, sec, s);
+    }
     return cudaGetLastError();
 }
 
@@ -1036,16 +1129,20 @@ void step_tile(int *tx, int *ty) {
 
 template <typename T>
 int tma_grid_items(int64_t items, int num_sms) {
-    Geom g;
-    memset(&g, 0, sizeof g);
-    g.nx = g.ny = g.nz = 1;
-    int zc = 1;
-    if (tma_grid<T>(g, num_sms, &zc) < 1) return -1;     // attributes + occupancy
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 1, true, false>,
-                                                      TmaGeo<T>::NT, tma_smem_bytes<T>()) != cudaSuccess ||
-        occ < 1)
-        occ = 1;
+    // kernel attributes of the ensemble variants are per device: set them once for each
+    static int occ_of[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+    int &occ = occ_of[dev];
+    if (!occ) {
+        if (set_attrs<T, true>() != cudaSuccess) return -1;
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 1, true, SET_WHOLE>,
+                                                          TmaGeo<T>::NT, tma_smem_bytes<T>()) != cudaSuccess ||
+            o < 1)
+            o = 1;
+        occ = o;
+    }
     const int64_t slots = (int64_t)occ * num_sms;
     return (int)(items < slots ? items : slots);
 }

@@ -15,8 +15,10 @@ struct alignas(128) DomainDesc {
     Geom g;
     void *fld[2][3];          // [buffer][etaS, etaL, c]
     int ntx, nty;             // tiles in x and y
+    int nfx, nfy;             // whole tiles (inside the domain) in x and y
     int zc, nc;               // z planes per work item, items per tile column
-    int item0, nitems;        // first work item of this domain in the ensemble, count
+    int item0[2], nitems[2];  // first work item and count of this domain in the ensemble's launch
+                              // over edge tiles [0] and over whole tiles [1]
 };
 
 // Launch choices of the fused step that the autotuner may change.
@@ -49,9 +51,9 @@ int tma_grid_for(const Geom &g, int num_sms, const StepTune &t);
 // (nullable) receives 3 doubles per work item (tma_items of them); `err` is
 // a device word that a CTA sets when an mbarrier wait exceeds limit_ns.
 // inject_stall != 0 is a test hook that makes one wait per CTA run out.
-// `sched` is the launch's scheduler word pair (two ints, zero before the
-// first launch; every launch leaves them zero), used when tune.sched is set;
-// launches that share a pair must be ordered on one stream.
+// `sched` points to the step's two scheduler word pairs (four ints, zero
+// before the first launch; every launch leaves them zero), used when
+// tune.sched is set; steps that share them must be ordered on one stream.
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
                             bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
@@ -70,12 +72,13 @@ template <typename T>
 int tma_grid_items(int64_t items, int num_sms);
 
 // One fused step of every domain of an ensemble: reads buffer `parity` of
-// each domain and writes buffer 1-parity.  `partials` (nullable) receives 3
-// doubles per work item (the last-step increment sums); `sched` (nullable)
-// as for launch_step_tma.
+// each domain and writes buffer 1-parity, as a launch over the whole tiles
+// (items[1] work items) and one over the edge tiles (items[0]).  `partials`
+// (nullable) receives 3 doubles per work item (the last-step increment
+// sums), the whole tiles' first; `sched` (nullable) as for launch_step_tma.
 template <typename T>
-cudaError_t launch_step_multi(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
-                              int parity, double *partials, int grid, int roll, int *err,
+cudaError_t launch_step_multi(const DomainDesc *table, int ndom, const int *items, const Coef<T> &k, bool c_only,
+                              bool eqA, int parity, double *partials, int grid, int roll, bool pdl, int *err,
                               unsigned long long limit_ns, int *sched, cudaStream_t s);
 
 }  // namespace ppf

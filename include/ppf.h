@@ -199,6 +199,10 @@ typedef struct ppf_tune {
                             planes instead of zc (short items end the step, so that its CTAs end
                             closer together); 0: every item zc planes */
     int tail;
+    int split;           /* 1 (the default): a domain whose x or y edge is not a multiple of the
+                            tile runs its whole tiles and its edge tiles as two launches, the
+                            second in the first one's tail (with pdl); 0: one launch over every
+                            tile.  Both give the same bits. */
     double us_per_step;  /* measured time of the winner (ppf_autotune only) */
 } ppf_tune;
 

@@ -35,6 +35,11 @@ static constexpr int kStepPdl = 1;
 // take more items and the launch's CTAs end closer together.
 static constexpr int kStepSched = 1;
 
+// A domain whose x or y edge is not a multiple of the tile runs its whole
+// tiles and its edge tiles as two launches, the second in the first one's
+// tail, unless the autotuner finds one launch over every tile faster.
+static constexpr int kStepSplit = 1;
+
 static int seterr(int code, const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -205,6 +210,7 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
     c->tune.roll = 1;
     c->tune.pdl = kStepPdl;
     c->tune.sched = kStepSched;
+    c->tune.split = kStepSplit;
     c->tune.grid = precision == PPF_F32 ? tma_grid<float>(c->g, c->num_sms, &c->tune.zc)
                                         : tma_grid<double>(c->g, c->num_sms, &c->tune.zc);
     if (c->tune.grid < 1) {
@@ -447,6 +453,7 @@ extern "C" int ppf_get_tune(const ppf_ctx *c, ppf_tune *t) {
     t->sched = c->tune.sched;
     t->zc2 = c->tune.zc2;
     t->tail = c->tune.tail;
+    t->split = c->tune.split;
     t->us_per_step = 0.0;
     return PPF_OK;
 }
@@ -458,12 +465,14 @@ extern "C" int ppf_set_tune(ppf_ctx *c, const ppf_tune *t) {
     if (t->pdl != 0 && t->pdl != 1) return seterr(PPF_EINVAL, "pdl must be 0 or 1");
     if (t->sched != 0 && t->sched != 1) return seterr(PPF_EINVAL, "sched must be 0 or 1");
     if (t->zc2 < 0 || t->tail < 0 || t->tail > c->nz) return seterr(PPF_EINVAL, "need zc2 >= 0 and 0 <= tail <= nz");
+    if (t->split != 0 && t->split != 1) return seterr(PPF_EINVAL, "split must be 0 or 1");
     CU(cudaStreamSynchronize(c->stream));
     StepTune n = c->tune;
     n.zc = t->zc;
     n.roll = t->roll;
     n.pdl = t->pdl;
     n.sched = t->sched;
+    n.split = t->split;
     n.zc2 = t->zc2 < t->zc ? t->zc2 : 0;
     n.tail = n.zc2 > 0 ? t->tail : 0;
     n.grid = grid_for(c, n);
@@ -532,12 +541,19 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
         cudaEventElapsedTime(&ms, e0, e1);
         if (best_ms < 0 || ms < best_ms) { best_ms = ms; win = t; }
     };
-    // uniform chunks
+    // uniform chunks; with edge tiles, as one launch or two
+    int tx = 0, ty = 0;
+    if (c->prec == PPF_F32) step_tile<float>(&tx, &ty);
+    else step_tile<double>(&tx, &ty);
+    const bool edges = c->nx % tx != 0 || c->ny % ty != 0, wholes = c->nx >= tx && c->ny >= ty;
+    const int nsplit = edges && wholes ? 2 : 1;
+    for (int sp = 0; sp < nsplit && rc == PPF_OK; ++sp)
     for (int sd = 1; sd >= 0 && rc == PPF_OK; --sd)
     for (int pdl = 1; pdl >= 0 && rc == PPF_OK; --pdl)
     for (int r = 0; r < 2 && rc == PPF_OK; ++r)
         for (int i = 0; i < nzc && rc == PPF_OK; ++i) {
             StepTune t = keep;
+            t.split = nsplit == 2 ? sp : keep.split;
             t.sched = sd;
             t.pdl = pdl;
             t.roll = r == 0 ? 3 : 1;
@@ -551,9 +567,6 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     // the persistent grid's items
     if (rc == PPF_OK && win.sched == 1) {
         const StepTune base = win;
-        int tx = 0, ty = 0;
-        if (c->prec == PPF_F32) step_tile<float>(&tx, &ty);
-        else step_tile<double>(&tx, &ty);
         const int64_t ntiles = (int64_t)((c->nx + tx - 1) / tx) * ((c->ny + ty - 1) / ty);
         const int64_t slots = grid_for(c, 1);
         int mains[5], nm = 0;
@@ -594,6 +607,7 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
         best->sched = win.sched;
         best->zc2 = win.zc2;
         best->tail = win.tail;
+        best->split = win.split;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }
     return PPF_OK;

@@ -38,17 +38,19 @@ int err_(int code, const char *fmt, ...) {
         if (e_ != cudaSuccess) return err_(PPF_ECUDA, "%s: %s", #call, cudaGetErrorString(e_));   \
     } while (0)
 
-// per-domain sums of the per-item increment partials (deterministic order):
-// the domain's whole-tile items, then its edge-tile items, which follow all
-// `nwhole` whole-tile items in `partials`
+// per-domain sums of the per-item increment partials (deterministic order).
+// nwhole < 0: the step was one launch over every tile (the domain's range
+// of it); else the domain's whole-tile items, then its edge-tile items,
+// which follow all `nwhole` whole-tile items in `partials`
 __global__ void domain_sums(const DomainDesc *__restrict__ table, const double *__restrict__ partials, int nwhole,
                             double *const *__restrict__ dres) {
     const DomainDesc &d = table[blockIdx.x];
     __shared__ double red[3][128];
     double a[3] = {0, 0, 0};
-    const int n = d.nitems[1] + d.nitems[0];
+    const int n = nwhole < 0 ? d.nitems[2] : d.nitems[1] + d.nitems[0];
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int64_t r = i < d.nitems[1] ? d.item0[1] + i : (int64_t)nwhole + d.item0[0] + (i - d.nitems[1]);
+        const int64_t r = nwhole < 0 ? (int64_t)d.item0[2] + i
+                          : i < d.nitems[1] ? d.item0[1] + i : (int64_t)nwhole + d.item0[0] + (i - d.nitems[1]);
         for (int v = 0; v < 3; ++v) a[v] += partials[r * 3 + v];
     }
     for (int v = 0; v < 3; ++v) red[v][threadIdx.x] = a[v];
@@ -72,7 +74,8 @@ struct ppf_ensemble {
     double **ddres;              // device: each domain's dres pointer
     double *partials;            // 3 doubles per work item
     int partials_cap;
-    int items[2];                // work items of the edge-tile [0] and whole-tile [1] launches
+    int items[3];                // work items of the edge-tile [0], whole-tile [1] and every-tile [2] launches
+    int split;                   // 1: whole and edge tiles as two overlapping launches; 0: one launch
     int grid, zc, roll;
     int pdl;                     // 1: launches overlap by programmatic dependent launch
     int sched;                   // 1: work items from a counter (domain 0's scheduler pair; the
@@ -92,7 +95,7 @@ static int build_table(ppf_ensemble *e) {
     if (e->prec == PPF_F32) step_tile<float>(&tx, &ty);
     else step_tile<double>(&tx, &ty);
     std::vector<DomainDesc> h((size_t)e->n);
-    int64_t item0s[2] = {0, 0};
+    int64_t item0s[3] = {0, 0, 0};
     for (int k = 0; k < e->n; ++k) {
         ppf_ctx *c = e->dom[(size_t)e->order[(size_t)k]];
         DomainDesc &t = h[(size_t)k];
@@ -111,7 +114,8 @@ static int build_table(ppf_ensemble *e) {
         t.nc = (c->nz + t.zc - 1) / t.zc;
         t.nitems[1] = t.nfx * t.nfy * t.nc;
         t.nitems[0] = (t.ntx * t.nty - t.nfx * t.nfy) * t.nc;
-        for (int q = 0; q < 2; ++q) {
+        t.nitems[2] = t.ntx * t.nty * t.nc;
+        for (int q = 0; q < 3; ++q) {
             t.item0[q] = (int)item0s[q];
             item0s[q] += t.nitems[q];
         }
@@ -119,7 +123,8 @@ static int build_table(ppf_ensemble *e) {
     if (item0s[0] + item0s[1] > ((int64_t)1 << 29)) return err_(PPF_EINVAL, "ensemble has too many work items");
     e->items[0] = (int)item0s[0];
     e->items[1] = (int)item0s[1];
-    const int64_t item0 = item0s[0] + item0s[1];
+    e->items[2] = (int)item0s[2];
+    const int64_t item0 = item0s[2];
     e->grid = e->prec == PPF_F32 ? tma_grid_items<float>(item0, e->num_sms) : tma_grid_items<double>(item0, e->num_sms);
     if (e->grid < 1) return err_(PPF_ECUDA, "no launch shape for the ensemble");
     ECU(cudaMemcpyAsync(e->dtable, h.data(), h.size() * sizeof(DomainDesc), cudaMemcpyHostToDevice, e->stream));
@@ -142,14 +147,12 @@ static int launch_one(ppf_ensemble *e, bool stats) {
     cudaError_t r;
     if (e->prec == PPF_F32)
         r = launch_step_multi<float>(e->dtable, e->n, e->items, c0->kf, false, e->eqA, e->parity,
-                                     stats ? e->partials : nullptr, e->grid, e->roll, e->pdl != 0, c0->derr,
-                                     c0->wait_limit_ns,
-                                     e->sched ? c0->dsched : nullptr, e->stream);
+                                     stats ? e->partials : nullptr, e->grid, e->roll, e->pdl != 0, e->split != 0,
+                                     c0->derr, c0->wait_limit_ns, e->sched ? c0->dsched : nullptr, e->stream);
     else
         r = launch_step_multi<double>(e->dtable, e->n, e->items, c0->kd, false, e->eqA, e->parity,
-                                      stats ? e->partials : nullptr, e->grid, e->roll, e->pdl != 0, c0->derr,
-                                      c0->wait_limit_ns,
-                                      e->sched ? c0->dsched : nullptr, e->stream);
+                                      stats ? e->partials : nullptr, e->grid, e->roll, e->pdl != 0, e->split != 0,
+                                      c0->derr, c0->wait_limit_ns, e->sched ? c0->dsched : nullptr, e->stream);
     if (r != cudaSuccess) return err_(PPF_ECUDA, "ensemble step launch: %s", cudaGetErrorString(r));
     e->parity ^= 1;
     return PPF_OK;
@@ -206,6 +209,7 @@ extern "C" int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, 
     e->roll = 1;
     e->sched = 1;
     e->pdl = 1;
+    e->split = 0;
     int rc = PPF_OK;
     for (int d = 0; d < n && rc == PPF_OK; ++d) {
         ppf_ctx *c = nullptr;
@@ -311,7 +315,9 @@ static int run(ppf_ensemble *e, int64_t nsteps) {
     }
     for (; left > 0 && rc == PPF_OK; --left) rc = launch_one(e, left == 1);
     if (rc) return rc;
-    domain_sums<<<e->n, 128, 0, e->stream>>>(e->dtable, e->partials, e->items[1], e->ddres);
+    // the layout of the statistics step's partials (launch_step_multi)
+    const int nwhole = e->items[0] == 0 || (e->split && e->items[1] > 0) ? e->items[1] : -1;
+    domain_sums<<<e->n, 128, 0, e->stream>>>(e->dtable, e->partials, nwhole, e->ddres);
     ECU(cudaGetLastError());
     for (ppf_ctx *x : e->dom) {
         x->cur_eta = x->cur_c = e->parity;
@@ -341,6 +347,7 @@ extern "C" int ppf_ensemble_get_tune(const ppf_ensemble *e, ppf_tune *t) {
     t->grid = e->grid;
     t->pdl = e->pdl;
     t->sched = e->sched;
+    t->split = e->split;
     t->zc2 = t->tail = 0;
     t->us_per_step = 0;
     return PPF_OK;
@@ -352,7 +359,9 @@ extern "C" int ppf_ensemble_set_tune(ppf_ensemble *e, const ppf_tune *t) {
     if (t->zc < 1) return err_(PPF_EINVAL, "zc must be >= 1");
     if (t->sched != 0 && t->sched != 1) return err_(PPF_EINVAL, "sched must be 0 or 1");
     if (t->pdl != 0 && t->pdl != 1) return err_(PPF_EINVAL, "pdl must be 0 or 1");
+    if (t->split != 0 && t->split != 1) return err_(PPF_EINVAL, "split must be 0 or 1");
     ECU(cudaStreamSynchronize(e->stream));
+    e->split = t->split;
     e->zc = t->zc;
     e->roll = t->roll;
     e->sched = t->sched;
@@ -370,13 +379,15 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
     for (ppf_ctx *x : e->dom)
         if ((rc = do_unpack(x)) != PPF_OK) return rc;
     const int zcs[] = {4, 8, 12, 16, 24, 32, 48, 64, 128};
-    const int keep_zc = e->zc, keep_roll = e->roll, keep_sched = e->sched, keep_pdl = e->pdl;
+    const int keep_zc = e->zc, keep_roll = e->roll, keep_sched = e->sched, keep_pdl = e->pdl, keep_split = e->split;
     const int64_t keep_steps = e->steps;
-    int best_zc = keep_zc, best_roll = keep_roll, best_sched = keep_sched, best_pdl = keep_pdl;
+    int best_zc = keep_zc, best_roll = keep_roll, best_sched = keep_sched, best_pdl = keep_pdl, best_split = keep_split;
+    const int nsplit = e->items[0] > 0 && e->items[1] > 0 ? 2 : 1;   // both kinds of tile: try both
     float best_ms = -1.0f;
     cudaEvent_t t0, t1;
     ECU(cudaEventCreate(&t0));
     ECU(cudaEventCreate(&t1));
+    for (int sp = 0; sp < nsplit && rc == PPF_OK; ++sp)
     for (int pdl = 1; pdl >= 0 && rc == PPF_OK; --pdl)
     for (int sd = 1; sd >= 0 && rc == PPF_OK; --sd)
     for (int r = 0; r < 2 && rc == PPF_OK; ++r)
@@ -385,6 +396,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
             e->roll = r == 0 ? 1 : 3;
             e->sched = sd;
             e->pdl = pdl;
+            e->split = sp;
             if ((rc = build_table(e)) != PPF_OK) break;
             for (int s = 0; s < 2 && rc == PPF_OK; ++s) rc = launch_one(e, false);     // warm-up
             if (rc) break;
@@ -401,6 +413,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
                 best_roll = e->roll;
                 best_sched = e->sched;
                 best_pdl = e->pdl;
+                best_split = e->split;
             }
         }
     cudaEventDestroy(t0);
@@ -409,6 +422,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
     e->roll = rc == PPF_OK ? best_roll : keep_roll;
     e->sched = rc == PPF_OK ? best_sched : keep_sched;
     e->pdl = rc == PPF_OK ? best_pdl : keep_pdl;
+    e->split = rc == PPF_OK ? best_split : keep_split;
     int rc2 = build_table(e);
     for (ppf_ctx *x : e->dom)
         if (rc2 == PPF_OK) {
@@ -427,6 +441,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
         best->grid = e->grid;
         best->pdl = e->pdl;
         best->sched = e->sched;
+        best->split = e->split;
         best->zc2 = best->tail = 0;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }

@@ -321,14 +321,15 @@ struct Item {
     int dom, bx, by, z0, z1;
 };
 
-// The tiles of one launch.  A step is run as up to two launches over
-// disjoint tile sets: the whole tiles (SET_WHOLE: the nfx x nfy rectangle
-// of tiles inside the domain, whose plane body needs no per-cell "inside"
-// test) and the edge tiles (SET_EDGE: the column of partial tiles at high x
-// when nx is not a multiple of the tile width, then the row of partial
-// tiles at high y), or, for a domain whose fields exceed 2^32 elements, one
-// launch over every tile with 64-bit offsets (SET_ALL).
-enum { SET_ALL = 0, SET_EDGE = 1, SET_WHOLE = 2 };
+// The tiles of one launch.  A step is one launch over every tile (SET_ALL;
+// SET_WIDE with 64-bit offsets, for a domain whose fields exceed 2^32
+// elements), or, when every tile lies inside the domain, over the whole
+// tiles (SET_WHOLE: the nfx x nfy rectangle of tiles inside the domain,
+// whose plane body needs no per-cell "inside" test), or two launches: the
+// whole tiles and the edge tiles (SET_EDGE: the column of partial tiles at
+// high x when nx is not a multiple of the tile width, then the row of
+// partial tiles at high y).
+enum { SET_WIDE = 0, SET_EDGE = 1, SET_WHOLE = 2, SET_ALL = 3 };
 
 struct Tiles {
     int ntx, nty;   // tiles in x and y
@@ -336,13 +337,13 @@ struct Tiles {
 };
 
 __host__ __device__ inline int tiles_in_set(const Tiles &t, int set) {
-    return set == SET_ALL ? t.ntx * t.nty : set == SET_WHOLE ? t.nfx * t.nfy : t.ntx * t.nty - t.nfx * t.nfy;
+    return set == SET_WHOLE ? t.nfx * t.nfy : set == SET_EDGE ? t.ntx * t.nty - t.nfx * t.nfy : t.ntx * t.nty;
 }
 
 // tile k of the set
 template <int SET>
 __device__ __forceinline__ void tile_of(int k, const Tiles &t, int &bx, int &by) {
-    if (SET == SET_ALL) {
+    if (SET == SET_ALL || SET == SET_WIDE) {
         by = k / t.ntx;
         bx = k - by * t.ntx;
     } else if (SET == SET_WHOLE) {
@@ -387,7 +388,7 @@ __device__ __forceinline__ Item item_at(int item, const Tiles &t1, const ZSplit 
         it.z1 = min(nz, it.z0 + (c < zs.n1 ? zs.zc : zs.zc2));
         return it;
     }
-    const int s = SET == SET_WHOLE ? 1 : 0;
+    const int s = SET == SET_WHOLE ? 1 : SET == SET_EDGE ? 0 : 2;
     int lo = 0, hi = ndom - 1;                 // last domain with item0 <= item
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -407,8 +408,8 @@ __device__ __forceinline__ Item item_at(int item, const Tiles &t1, const ZSplit 
 }
 
 // SET: the launch's tiles (SET_WHOLE: no per-cell "inside the domain" test;
-// SET_EDGE: with it; SET_ALL: with it and 64-bit element offsets, for fields
-// of more than 2^32 elements; the other sets use 32-bit offsets).
+// SET_EDGE, SET_ALL: with it; SET_WIDE: with it and 64-bit element offsets,
+// for fields of more than 2^32 elements; the other sets use 32-bit offsets).
 template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL, bool MULTI, int SET>
 __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
@@ -443,7 +444,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
     const int ty0 = (warp / G::WX) * CY;              // first own row in the tile
     const int nitems = mitems;
     const int ob = (ty0 + 1) * BX + tx + XH;          // shared offset of the first own cell
-    static_assert(!(MULTI && SET == SET_ALL), "ensemble domains hold fewer than 2^32 elements per field");
+    static_assert(!(MULTI && SET == SET_WIDE), "ensemble domains hold fewer than 2^32 elements per field");
     constexpr bool FULL = SET == SET_WHOLE;
     // the pair of cells of the one-cell ring around the tile that this thread
     // evaluates: the last RING/2 threads (warp 0 also feeds the TMA ring), each
@@ -634,7 +635,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                     const T *nS = sm.raw[st_prev][0], *nL = sm.raw[st_prev][1];
                     const T *nmu = sm.mm[mb_prev][0], *nM = sm.mm[mb_prev][1];
                     // 32-bit element offsets unless the fields exceed 2^32 elements
-                    using Off = typename std::conditional<SET == SET_ALL, int64_t, uint32_t>::type;
+                    using Off = typename std::conditional<SET == SET_WIDE, int64_t, uint32_t>::type;
                     const Off base = (Off)col + (Off)(q + 1) * (Off)g.PS;
                     // the new values of the plane's own cells, kept for the face ghosts below
                     V2<T> gS[H], gL[H], gC[H];
@@ -863,14 +864,15 @@ static cudaError_t set_attr1() {
     const int sh = (int)tma_smem_bytes<T>();
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e;
-    if (M) {
-        if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, true, SET_EDGE>, a, sh))) return e;
-        return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, true, SET_WHOLE>, a, sh);
+    // (the plane body is unrolled three times only for whole tiles)
+    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, M, SET_WHOLE>, a, sh))) return e;
+    if constexpr (R == 1) {
+        if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, 1, M, SET_EDGE>, a, sh)) ||
+            (e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, 1, M, SET_ALL>, a, sh)))
+            return e;
+        if constexpr (!M) return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, 1, false, SET_WIDE>, a, sh);
     }
-    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, SET_ALL>, a, sh)) ||
-        (e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, SET_EDGE>, a, sh)))
-        return e;
-    return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, false, SET_WHOLE>, a, sh);
+    return cudaSuccess;
 }
 
 template <typename T, int R, bool M>
@@ -1044,22 +1046,29 @@ static void launch_sets(const Geom &g, const Coef<T> &k, const CUtensorMap *maps
                         int inject_stall, int *sched, cudaStream_t s) {
     const Tiles t = tiles_of<T>(g);
     const int64_t chunks = tma_items<T>(g, tune) / ((int64_t)t.ntx * t.nty);
+    const int na = (int)(chunks * t.ntx * t.nty);
     if (g.total > ((int64_t)1 << 32)) {        // 64-bit offsets: one launch over every tile
-        launch_r<T, R, SET_ALL>(g, k, maps, out, c_only, eqA, partials, tune, (int)(chunks * t.ntx * t.nty), err,
-                                limit_ns, inject_stall, sched, 0, s);
+        launch_r<T, 1, SET_WIDE>(g, k, maps, out, c_only, eqA, partials, tune, na, err, limit_ns, inject_stall, sched,
+                                 0, s);
+        return;
+    }
+    const int nw = (int)(chunks * tiles_in_set(t, SET_WHOLE)), ne = (int)(chunks * tiles_in_set(t, SET_EDGE));
+    if (ne == 0) {                             // every tile inside the domain
+        launch_r<T, R, SET_WHOLE>(g, k, maps, out, c_only, eqA, partials, tune, nw, err, limit_ns, inject_stall, sched,
+                                  0, s);
+        return;
+    }
+    if (!tune.split || nw == 0) {              // one launch over every tile
+        launch_r<T, 1, SET_ALL>(g, k, maps, out, c_only, eqA, partials, tune, na, err, limit_ns, inject_stall, sched,
+                                0, s);
         return;
     }
     // the whole tiles, then the edge tiles (their increment sums follow the
     // whole tiles' in `partials`; their own scheduler pair, since the two
     // launches overlap)
-    const int nw = (int)(chunks * tiles_in_set(t, SET_WHOLE)), ne = (int)(chunks * tiles_in_set(t, SET_EDGE));
-    if (nw > 0)
-        launch_r<T, R, SET_WHOLE>(g, k, maps, out, c_only, eqA, partials, tune, nw, err, limit_ns, inject_stall, sched,
-                                  0, s);
-    if (ne > 0)
-        launch_r<T, R, SET_EDGE>(g, k, maps, out, c_only, eqA, partials ? partials + 3 * (int64_t)nw : nullptr, tune,
-                                 ne, err, limit_ns, nw > 0 ? 0 : inject_stall, sched ? sched + 2 : nullptr,
-                                 nw > 0 ? 1 : 0, s);
+    launch_r<T, R, SET_WHOLE>(g, k, maps, out, c_only, eqA, partials, tune, nw, err, limit_ns, inject_stall, sched, 0, s);
+    launch_r<T, 1, SET_EDGE>(g, k, maps, out, c_only, eqA, partials ? partials + 3 * (int64_t)nw : nullptr, tune, ne,
+                             err, limit_ns, 0, sched ? sched + 2 : nullptr, 1, s);
 }
 
 template <typename T>
@@ -1102,22 +1111,25 @@ static void launch_multi_r(const DomainDesc *table, int ndom, int items, const C
 
 template <typename T>
 cudaError_t launch_step_multi(const DomainDesc *table, int ndom, const int *items, const Coef<T> &k, bool c_only,
-                              bool eqA, int parity, double *partials, int grid, int roll, bool pdl, int *err,
-                              unsigned long long limit_ns, int *sched, cudaStream_t s) {
+                              bool eqA, int parity, double *partials, int grid, int roll, bool pdl, bool split,
+                              int *err, unsigned long long limit_ns, int *sched, cudaStream_t s) {
+    const int nw = items[1], ne = items[0], na = items[2];
+    if (ne == 0) {                             // every tile of every domain inside its domain
+        if (roll == 1) launch_multi_r<T, 1, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
+        else launch_multi_r<T, 3, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
+        return cudaGetLastError();
+    }
+    if (!split || nw == 0) {                   // one launch over every tile
+        launch_multi_r<T, 1, SET_ALL>(table, ndom, na, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
+        return cudaGetLastError();
+    }
     // the whole tiles of every domain, then the edge tiles (their increment
     // sums follow the whole tiles' in `partials`; their own scheduler pair,
     // since the two launches overlap)
-    const int nw = items[1], ne = items[0];
-    double *pe = partials ? partials + 3 * (int64_t)nw : nullptr;
-    int *se = sched ? sched + 2 : nullptr;
-    const int sec = nw > 0 ? 1 : 0;
-    if (roll == 1) {
-        if (nw > 0) launch_multi_r<T, 1, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
-        if (ne > 0) launch_multi_r<T, 1, SET_EDGE>(table, ndom, ne, k, c_only, eqA, parity, pe, grid, err, limit_ns, se, pdl, sec, s);
-    } else {
-        if (nw > 0) launch_multi_r<T, 3, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
-        if (ne > 0) launch_multi_r<T, 3, SET_EDGE>(table, ndom, ne, k, c_only, eqA, parity, pe, grid, err, limit_ns, se, pdl, sec, s);
-    }
+    if (roll == 1) launch_multi_r<T, 1, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
+    else launch_multi_r<T, 3, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
+    launch_multi_r<T, 1, SET_EDGE>(table, ndom, ne, k, c_only, eqA, parity, partials ? partials + 3 * (int64_t)nw : nullptr,
+                                   grid, err, limit_ns, sched ? sched + 2 : nullptr, pdl, 1, s);
     return cudaGetLastError();
 }
 

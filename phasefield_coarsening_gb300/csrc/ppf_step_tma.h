@@ -17,8 +17,8 @@ struct alignas(128) DomainDesc {
     int ntx, nty;             // tiles in x and y
     int nfx, nfy;             // whole tiles (inside the domain) in x and y
     int zc, nc;               // z planes per work item, items per tile column
-    int item0[2], nitems[2];  // first work item and count of this domain in the ensemble's launch
-                              // over edge tiles [0] and over whole tiles [1]
+    int item0[3], nitems[3];  // first work item and count of this domain in the ensemble's launch
+                              // over edge tiles [0], over whole tiles [1], over every tile [2]
 };
 
 // Launch choices of the fused step that the autotuner may change.
@@ -30,6 +30,7 @@ struct StepTune {
     int sched;  // 1: CTAs take work items from a global counter; 0: round-robin
     int zc2;    // > 0 (and < zc): the top `tail` planes are cut into chunks of zc2
     int tail;
+    int split;  // 1: whole tiles and edge tiles as two overlapping launches; 0: one launch
 };
 
 // Tensor map of one padded field (3-D: x pitch, ny+2 rows, nz+2 planes)
@@ -72,13 +73,14 @@ template <typename T>
 int tma_grid_items(int64_t items, int num_sms);
 
 // One fused step of every domain of an ensemble: reads buffer `parity` of
-// each domain and writes buffer 1-parity, as a launch over the whole tiles
-// (items[1] work items) and one over the edge tiles (items[0]).  `partials`
-// (nullable) receives 3 doubles per work item (the last-step increment
-// sums), the whole tiles' first; `sched` (nullable) as for launch_step_tma.
+// each domain and writes buffer 1-parity, as one launch over every tile
+// (items[2] work items), or with `split` a launch over the whole tiles
+// (items[1]) and one over the edge tiles (items[0]).  `partials` (nullable)
+// receives 3 doubles per work item (the last-step increment sums; with the
+// split the whole tiles' first); `sched` (nullable) as for launch_step_tma.
 template <typename T>
 cudaError_t launch_step_multi(const DomainDesc *table, int ndom, const int *items, const Coef<T> &k, bool c_only,
-                              bool eqA, int parity, double *partials, int grid, int roll, bool pdl, int *err,
-                              unsigned long long limit_ns, int *sched, cudaStream_t s);
+                              bool eqA, int parity, double *partials, int grid, int roll, bool pdl, bool split,
+                              int *err, unsigned long long limit_ns, int *sched, cudaStream_t s);
 
 }  // namespace ppf

@@ -319,7 +319,8 @@ def run_ours(args):
     sim2 = ppf.Simulation(shape, ppf.params_default(dt=DT), bc="periodic", precision="f32")
     stream2 = torch.cuda.Stream()
     sim2.set_stream(stream2.cuda_stream)
-    sim2.set_tune(tune["zc"], tune["roll"], tune["pdl"], tune["sched"], tune["zc2"], tune["tail"], tune["split"])
+    sim2.set_tune(tune["zc"], tune["roll"], tune["pdl"], tune["sched"], tune["zc2"], tune["tail"], tune["split"],
+                  tune["tile"])
     host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (eS, eL, c)]
     outh = [[torch.empty(shape, dtype=torch.float64).pin_memory() for _ in range(3)] for _ in range(2)]
     ptr_in = [h.data_ptr() for h in host]
@@ -501,7 +502,7 @@ def run_ensemble(args):
     # thread each, take alternate bench steps so that one's host-link copies
     # overlap the other's stepping (as in the single-domain line).
     ens2 = ppf.Ensemble(shapes, prm, bc="periodic", precision="f32")
-    ens2.set_tune(tune["zc"], tune["roll"], tune["sched"], tune["pdl"], tune["split"])
+    ens2.set_tune(tune["zc"], tune["roll"], tune["sched"], tune["pdl"], tune["split"], tune["tile"])
     L = ppf.lib()
     pin_in = [[torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in d[:3]] for d in doms]
     pin_out = [[[torch.empty(s, dtype=torch.float64).pin_memory() for _ in range(3)] for s in shapes]

@@ -203,6 +203,8 @@ typedef struct ppf_tune {
                             tile runs its whole tiles and its edge tiles as two launches, the
                             second in the first one's tail (with pdl); 0: one launch over every
                             tile.  Both give the same bits. */
+    int tile;            /* tile shape of a work item's brick: 0 (the default) 64 x 16 cells in x, y;
+                            1 (FP32 only) 32 x 32.  All give the same bits. */
     double us_per_step;  /* measured time of the winner (ppf_autotune only) */
 } ppf_tune;
 

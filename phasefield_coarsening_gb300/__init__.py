@@ -72,7 +72,7 @@ class Tune(ctypes.Structure):
     """ppf_tune: launch choices of the fused step."""
     _fields_ = [("zc", ctypes.c_int), ("roll", ctypes.c_int), ("grid", ctypes.c_int), ("pdl", ctypes.c_int),
                 ("sched", ctypes.c_int), ("zc2", ctypes.c_int), ("tail", ctypes.c_int), ("split", ctypes.c_int),
-                ("us_per_step", ctypes.c_double)]
+                ("tile", ctypes.c_int), ("us_per_step", ctypes.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -291,8 +291,8 @@ class Simulation:
         return t.as_dict()
 
     def set_tune(self, zc: int, roll: int = 1, pdl: int = 1, sched: int = 1, zc2: int = 0, tail: int = 0,
-                 split: int = 1):
-        t = Tune(int(zc), int(roll), 0, int(pdl), int(sched), int(zc2), int(tail), int(split), 0.0)
+                 split: int = 1, tile: int = 0):
+        t = Tune(int(zc), int(roll), 0, int(pdl), int(sched), int(zc2), int(tail), int(split), int(tile), 0.0)
         _check(lib().ppf_set_tune(self._h, ctypes.byref(t)))
 
     def particles(self, threshold: float = 0.5, volumes: bool = False) -> dict:
@@ -474,8 +474,8 @@ class Ensemble:
         _check(lib().ppf_ensemble_get_tune(self._h, ctypes.byref(t)))
         return t.as_dict()
 
-    def set_tune(self, zc: int, roll: int = 1, sched: int = 1, pdl: int = 1, split: int = 0):
-        t = Tune(int(zc), int(roll), 0, int(pdl), int(sched), 0, 0, int(split), 0.0)
+    def set_tune(self, zc: int, roll: int = 1, sched: int = 1, pdl: int = 1, split: int = 0, tile: int = 0):
+        t = Tune(int(zc), int(roll), 0, int(pdl), int(sched), 0, 0, int(split), int(tile), 0.0)
         _check(lib().ppf_ensemble_set_tune(self._h, ctypes.byref(t)))
 
     def autotune(self, trial_steps: int = 5) -> dict:

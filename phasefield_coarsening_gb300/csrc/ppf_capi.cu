@@ -198,15 +198,18 @@ extern "C" int ppf_create(int nz, int ny, int nx, const ppf_params *p, int bc, i
     c->wait_limit_ns = 1000000000ULL;
     for (int b = 0; b < 2; ++b)
         for (int f = 0; f < 3; ++f) c->fld[b][f] = (char *)c->state + (size_t)(3 * b + f) * fbytes;
-    for (int b = 0; b < 2 && rc == PPF_OK; ++b)
-        for (int f = 0; f < 3; ++f) {
-            int mr = precision == PPF_F32 ? make_field_map<float>(c->g, (const float *)c->fld[b][f], &c->maps[b][f])
-                                          : make_field_map<double>(c->g, (const double *)c->fld[b][f], &c->maps[b][f]);
-            if (mr != 0) {
-                ppf_destroy(c);
-                return seterr(PPF_ECUDA, "TMA descriptor setup failed (%d)", mr);
+    for (int tl = 0; tl < 2 && rc == PPF_OK; ++tl)
+        for (int b = 0; b < 2; ++b)
+            for (int f = 0; f < 3; ++f) {
+                // (FP64 has one tile shape: its second set repeats the first)
+                CUtensorMap *m = &c->maps[tl][b][f];
+                int mr = precision == PPF_F32 ? make_field_map<float>(c->g, (const float *)c->fld[b][f], m, tl)
+                                              : make_field_map<double>(c->g, (const double *)c->fld[b][f], m, 0);
+                if (mr != 0) {
+                    ppf_destroy(c);
+                    return seterr(PPF_ECUDA, "TMA descriptor setup failed (%d)", mr);
+                }
             }
-        }
     c->tune.roll = 1;
     c->tune.pdl = kStepPdl;
     c->tune.sched = kStepSched;
@@ -361,11 +364,12 @@ static int run_steps(ppf_ctx *c, int64_t nsteps, bool c_only) {
         c->inject = PPF_INJECT_NONE;
         cudaError_t e;
         if (c->prec == PPF_F32) {
-            const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
+            const int tl = c->tune.tile;
+            const CUtensorMap m[3] = {c->maps[tl][ie][0], c->maps[tl][ie][1], c->maps[tl][ic][2]};
             e = launch_step_tma<float>(c->g, c->kf, m, ff(c, oe, oc), c_only, c->eqA, part, c->tune,
                                        c->derr, c->wait_limit_ns, inject, c->dsched, c->stream);
         } else {
-            const CUtensorMap m[3] = {c->maps[ie][0], c->maps[ie][1], c->maps[ic][2]};
+            const CUtensorMap m[3] = {c->maps[0][ie][0], c->maps[0][ie][1], c->maps[0][ic][2]};
             e = launch_step_tma<double>(c->g, c->kd, m, fd(c, oe, oc), c_only, c->eqA, part, c->tune,
                                         c->derr, c->wait_limit_ns, inject, c->dsched, c->stream);
         }
@@ -454,6 +458,7 @@ extern "C" int ppf_get_tune(const ppf_ctx *c, ppf_tune *t) {
     t->zc2 = c->tune.zc2;
     t->tail = c->tune.tail;
     t->split = c->tune.split;
+    t->tile = c->tune.tile;
     t->us_per_step = 0.0;
     return PPF_OK;
 }
@@ -466,6 +471,8 @@ extern "C" int ppf_set_tune(ppf_ctx *c, const ppf_tune *t) {
     if (t->sched != 0 && t->sched != 1) return seterr(PPF_EINVAL, "sched must be 0 or 1");
     if (t->zc2 < 0 || t->tail < 0 || t->tail > c->nz) return seterr(PPF_EINVAL, "need zc2 >= 0 and 0 <= tail <= nz");
     if (t->split != 0 && t->split != 1) return seterr(PPF_EINVAL, "split must be 0 or 1");
+    const int shapes = c->prec == PPF_F32 ? step_tile_shapes<float>() : step_tile_shapes<double>();
+    if (t->tile < 0 || t->tile >= shapes) return seterr(PPF_EINVAL, "tile must be in [0, %d)", shapes);
     CU(cudaStreamSynchronize(c->stream));
     StepTune n = c->tune;
     n.zc = t->zc;
@@ -473,6 +480,7 @@ extern "C" int ppf_set_tune(ppf_ctx *c, const ppf_tune *t) {
     n.pdl = t->pdl;
     n.sched = t->sched;
     n.split = t->split;
+    n.tile = t->tile;
     n.zc2 = t->zc2 < t->zc ? t->zc2 : 0;
     n.tail = n.zc2 > 0 ? t->tail : 0;
     n.grid = grid_for(c, n);
@@ -506,8 +514,8 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
     add(c->tune.zc * 2);
     {
         int tx = 0, ty = 0;
-        if (c->prec == PPF_F32) step_tile<float>(&tx, &ty);
-        else step_tile<double>(&tx, &ty);
+        if (c->prec == PPF_F32) step_tile<float>(&tx, &ty, 0);
+        else step_tile<double>(&tx, &ty, 0);
         const int64_t ntiles = (int64_t)((c->nx + tx - 1) / tx) * ((c->ny + ty - 1) / ty);
         const int64_t slots = grid_for(c, 1);          // a grid that every CTA slot holds
         for (int k = 3; k <= 7 && ntiles > 0 && slots > 0; ++k) {
@@ -541,32 +549,41 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
         cudaEventElapsedTime(&ms, e0, e1);
         if (best_ms < 0 || ms < best_ms) { best_ms = ms; win = t; }
     };
-    // uniform chunks; with edge tiles, as one launch or two
-    int tx = 0, ty = 0;
-    if (c->prec == PPF_F32) step_tile<float>(&tx, &ty);
-    else step_tile<double>(&tx, &ty);
-    const bool edges = c->nx % tx != 0 || c->ny % ty != 0, wholes = c->nx >= tx && c->ny >= ty;
-    const int nsplit = edges && wholes ? 2 : 1;
-    for (int sp = 0; sp < nsplit && rc == PPF_OK; ++sp)
-    for (int sd = 1; sd >= 0 && rc == PPF_OK; --sd)
-    for (int pdl = 1; pdl >= 0 && rc == PPF_OK; --pdl)
-    for (int r = 0; r < 2 && rc == PPF_OK; ++r)
-        for (int i = 0; i < nzc && rc == PPF_OK; ++i) {
-            StepTune t = keep;
-            t.split = nsplit == 2 ? sp : keep.split;
-            t.sched = sd;
-            t.pdl = pdl;
-            t.roll = r == 0 ? 3 : 1;
-            t.zc = zcs[i];
-            t.zc2 = t.tail = 0;
-            trial(t);
-        }
+    // uniform chunks; with edge tiles, as one launch or two; the first tile
+    // shape with every deal and overlap, the others with the counter's deal
+    // and programmatic dependent launch
+    const int shapes = c->prec == PPF_F32 ? step_tile_shapes<float>() : step_tile_shapes<double>();
+    for (int tl = 0; tl < shapes && rc == PPF_OK; ++tl) {
+        int tx = 0, ty = 0;
+        if (c->prec == PPF_F32) step_tile<float>(&tx, &ty, tl);
+        else step_tile<double>(&tx, &ty, tl);
+        const bool edges = c->nx % tx != 0 || c->ny % ty != 0, wholes = c->nx >= tx && c->ny >= ty;
+        const int nsplit = edges && wholes ? 2 : 1;
+        for (int sp = 0; sp < nsplit && rc == PPF_OK; ++sp)
+        for (int sd = 1; sd >= (tl == 0 ? 0 : 1) && rc == PPF_OK; --sd)
+        for (int pdl = 1; pdl >= (tl == 0 ? 0 : 1) && rc == PPF_OK; --pdl)
+        for (int r = 0; r < 2 && rc == PPF_OK; ++r)
+            for (int i = 0; i < nzc && rc == PPF_OK; ++i) {
+                StepTune t = keep;
+                t.tile = tl;
+                t.split = nsplit == 2 ? sp : keep.split;
+                t.sched = sd;
+                t.pdl = pdl;
+                t.roll = r == 0 ? 3 : 1;
+                t.zc = zcs[i];
+                t.zc2 = t.tail = 0;
+                trial(t);
+            }
+    }
     // with the counter's deal: longer main chunks (the winner's and longer
     // ones, which pay fewer halo planes) with chunks of a half to a quarter
     // of their length at the top of z, covering about one or two waves of
     // the persistent grid's items
     if (rc == PPF_OK && win.sched == 1) {
         const StepTune base = win;
+        int tx = 0, ty = 0;
+        if (c->prec == PPF_F32) step_tile<float>(&tx, &ty, base.tile);
+        else step_tile<double>(&tx, &ty, base.tile);
         const int64_t ntiles = (int64_t)((c->nx + tx - 1) / tx) * ((c->ny + ty - 1) / ty);
         const int64_t slots = grid_for(c, 1);
         int mains[5], nm = 0;
@@ -608,6 +625,7 @@ extern "C" int ppf_autotune(ppf_ctx *c, int trial_steps, ppf_tune *best) {
         best->zc2 = win.zc2;
         best->tail = win.tail;
         best->split = win.split;
+        best->tile = win.tile;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }
     return PPF_OK;

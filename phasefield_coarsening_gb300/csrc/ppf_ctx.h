@@ -29,7 +29,7 @@ struct ppf_ctx {
                           // [16..19] mass-projection plan; the error word follows at dres + 32
     int *derr;            // device error word set by a kernel whose bounded wait ran out
     int *dsched;          // the step's two scheduler word pairs (dres + 32, after the error word)
-    CUtensorMap maps[2][3];   // TMA maps of the fields of both buffers
+    CUtensorMap maps[2][2][3];   // TMA maps of the fields of both buffers, per tile shape [tile][buffer][field]
     ppf::StepTune tune;        // launch choices of the fused step (grid, z chunk, unroll)
     unsigned long long wait_limit_ns;
     int inject;           // test hook: PPF_INJECT_*

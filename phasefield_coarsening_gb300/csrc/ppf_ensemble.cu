@@ -76,6 +76,7 @@ struct ppf_ensemble {
     int partials_cap;
     int items[3];                // work items of the edge-tile [0], whole-tile [1] and every-tile [2] launches
     int split;                   // 1: whole and edge tiles as two overlapping launches; 0: one launch
+    int tile;                    // tile shape
     int grid, zc, roll;
     int pdl;                     // 1: launches overlap by programmatic dependent launch
     int sched;                   // 1: work items from a counter (domain 0's scheduler pair; the
@@ -92,8 +93,8 @@ static constexpr int kGraphSteps = 16;
 
 static int build_table(ppf_ensemble *e) {
     int tx = 0, ty = 0;
-    if (e->prec == PPF_F32) step_tile<float>(&tx, &ty);
-    else step_tile<double>(&tx, &ty);
+    if (e->prec == PPF_F32) step_tile<float>(&tx, &ty, e->tile);
+    else step_tile<double>(&tx, &ty, e->tile);
     std::vector<DomainDesc> h((size_t)e->n);
     int64_t item0s[3] = {0, 0, 0};
     for (int k = 0; k < e->n; ++k) {
@@ -102,7 +103,7 @@ static int build_table(ppf_ensemble *e) {
         memset(&t, 0, sizeof t);
         for (int b = 0; b < 2; ++b)
             for (int f = 0; f < 3; ++f) {
-                t.maps[b][f] = c->maps[b][f];
+                t.maps[b][f] = c->maps[e->prec == PPF_F32 ? e->tile : 0][b][f];
                 t.fld[b][f] = c->fld[b][f];
             }
         t.g = c->g;
@@ -125,7 +126,8 @@ static int build_table(ppf_ensemble *e) {
     e->items[1] = (int)item0s[1];
     e->items[2] = (int)item0s[2];
     const int64_t item0 = item0s[2];
-    e->grid = e->prec == PPF_F32 ? tma_grid_items<float>(item0, e->num_sms) : tma_grid_items<double>(item0, e->num_sms);
+    e->grid = e->prec == PPF_F32 ? tma_grid_items<float>(item0, e->num_sms, e->tile)
+                                 : tma_grid_items<double>(item0, e->num_sms, 0);
     if (e->grid < 1) return err_(PPF_ECUDA, "no launch shape for the ensemble");
     ECU(cudaMemcpyAsync(e->dtable, h.data(), h.size() * sizeof(DomainDesc), cudaMemcpyHostToDevice, e->stream));
     if (3 * item0 > e->partials_cap) {
@@ -148,11 +150,11 @@ static int launch_one(ppf_ensemble *e, bool stats) {
     if (e->prec == PPF_F32)
         r = launch_step_multi<float>(e->dtable, e->n, e->items, c0->kf, false, e->eqA, e->parity,
                                      stats ? e->partials : nullptr, e->grid, e->roll, e->pdl != 0, e->split != 0,
-                                     c0->derr, c0->wait_limit_ns, e->sched ? c0->dsched : nullptr, e->stream);
+                                     e->tile, c0->derr, c0->wait_limit_ns, e->sched ? c0->dsched : nullptr, e->stream);
     else
         r = launch_step_multi<double>(e->dtable, e->n, e->items, c0->kd, false, e->eqA, e->parity,
                                       stats ? e->partials : nullptr, e->grid, e->roll, e->pdl != 0, e->split != 0,
-                                      c0->derr, c0->wait_limit_ns, e->sched ? c0->dsched : nullptr, e->stream);
+                                      0, c0->derr, c0->wait_limit_ns, e->sched ? c0->dsched : nullptr, e->stream);
     if (r != cudaSuccess) return err_(PPF_ECUDA, "ensemble step launch: %s", cudaGetErrorString(r));
     e->parity ^= 1;
     return PPF_OK;
@@ -210,6 +212,7 @@ extern "C" int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, 
     e->sched = 1;
     e->pdl = 1;
     e->split = 0;
+    e->tile = 0;
     int rc = PPF_OK;
     for (int d = 0; d < n && rc == PPF_OK; ++d) {
         ppf_ctx *c = nullptr;
@@ -348,6 +351,7 @@ extern "C" int ppf_ensemble_get_tune(const ppf_ensemble *e, ppf_tune *t) {
     t->pdl = e->pdl;
     t->sched = e->sched;
     t->split = e->split;
+    t->tile = e->tile;
     t->zc2 = t->tail = 0;
     t->us_per_step = 0;
     return PPF_OK;
@@ -360,6 +364,9 @@ extern "C" int ppf_ensemble_set_tune(ppf_ensemble *e, const ppf_tune *t) {
     if (t->sched != 0 && t->sched != 1) return err_(PPF_EINVAL, "sched must be 0 or 1");
     if (t->pdl != 0 && t->pdl != 1) return err_(PPF_EINVAL, "pdl must be 0 or 1");
     if (t->split != 0 && t->split != 1) return err_(PPF_EINVAL, "split must be 0 or 1");
+    const int shapes = e->prec == PPF_F32 ? step_tile_shapes<float>() : step_tile_shapes<double>();
+    if (t->tile < 0 || t->tile >= shapes) return err_(PPF_EINVAL, "tile must be in [0, %d)", shapes);
+    e->tile = t->tile;
     ECU(cudaStreamSynchronize(e->stream));
     e->split = t->split;
     e->zc = t->zc;
@@ -380,16 +387,26 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
         if ((rc = do_unpack(x)) != PPF_OK) return rc;
     const int zcs[] = {4, 8, 12, 16, 24, 32, 48, 64, 128};
     const int keep_zc = e->zc, keep_roll = e->roll, keep_sched = e->sched, keep_pdl = e->pdl, keep_split = e->split;
+    const int keep_tile = e->tile;
     const int64_t keep_steps = e->steps;
     int best_zc = keep_zc, best_roll = keep_roll, best_sched = keep_sched, best_pdl = keep_pdl, best_split = keep_split;
-    const int nsplit = e->items[0] > 0 && e->items[1] > 0 ? 2 : 1;   // both kinds of tile: try both
+    int best_tile = keep_tile;
+    const int shapes = e->prec == PPF_F32 ? step_tile_shapes<float>() : step_tile_shapes<double>();
     float best_ms = -1.0f;
     cudaEvent_t t0, t1;
     ECU(cudaEventCreate(&t0));
     ECU(cudaEventCreate(&t1));
+    // every tile shape; both kinds of tile: one launch or two; the first
+    // shape with every deal and overlap, the others with the counter's deal
+    // and programmatic dependent launch
+    for (int tl = 0; tl < shapes && rc == PPF_OK; ++tl) {
+    e->tile = tl;
+    e->zc = zcs[0];
+    if ((rc = build_table(e)) != PPF_OK) break;
+    const int nsplit = e->items[0] > 0 && e->items[1] > 0 ? 2 : 1;
     for (int sp = 0; sp < nsplit && rc == PPF_OK; ++sp)
-    for (int pdl = 1; pdl >= 0 && rc == PPF_OK; --pdl)
-    for (int sd = 1; sd >= 0 && rc == PPF_OK; --sd)
+    for (int pdl = 1; pdl >= (tl == 0 ? 0 : 1) && rc == PPF_OK; --pdl)
+    for (int sd = 1; sd >= (tl == 0 ? 0 : 1) && rc == PPF_OK; --sd)
     for (int r = 0; r < 2 && rc == PPF_OK; ++r)
         for (int zc : zcs) {
             e->zc = zc;
@@ -397,6 +414,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
             e->sched = sd;
             e->pdl = pdl;
             e->split = sp;
+            e->tile = tl;
             if ((rc = build_table(e)) != PPF_OK) break;
             for (int s = 0; s < 2 && rc == PPF_OK; ++s) rc = launch_one(e, false);     // warm-up
             if (rc) break;
@@ -414,8 +432,10 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
                 best_sched = e->sched;
                 best_pdl = e->pdl;
                 best_split = e->split;
+                best_tile = e->tile;
             }
         }
+    }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     e->zc = rc == PPF_OK ? best_zc : keep_zc;
@@ -423,6 +443,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
     e->sched = rc == PPF_OK ? best_sched : keep_sched;
     e->pdl = rc == PPF_OK ? best_pdl : keep_pdl;
     e->split = rc == PPF_OK ? best_split : keep_split;
+    e->tile = rc == PPF_OK ? best_tile : keep_tile;
     int rc2 = build_table(e);
     for (ppf_ctx *x : e->dom)
         if (rc2 == PPF_OK) {
@@ -442,6 +463,7 @@ extern "C" int ppf_ensemble_autotune(ppf_ensemble *e, int trial_steps, ppf_tune 
         best->pdl = e->pdl;
         best->sched = e->sched;
         best->split = e->split;
+        best->tile = e->tile;
         best->zc2 = best->tail = 0;
         best->us_per_step = best_ms * 1000.0 / trial_steps;
     }

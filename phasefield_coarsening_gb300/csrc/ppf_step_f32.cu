@@ -5,8 +5,9 @@
 
 namespace ppf {
 
-template void step_tile<float>(int *, int *);
-template int make_field_map<float>(const Geom &, const float *, CUtensorMap *);
+template void step_tile<float>(int *, int *, int);
+template int step_tile_shapes<float>();
+template int make_field_map<float>(const Geom &, const float *, CUtensorMap *, int);
 template int tma_grid<float>(const Geom &, int, int *);
 template int tma_grid_for<float>(const Geom &, int, const StepTune &);
 template int64_t tma_items<float>(const Geom &, const StepTune &);

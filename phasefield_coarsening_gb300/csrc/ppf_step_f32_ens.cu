@@ -4,9 +4,10 @@
 
 namespace ppf {
 
-template int tma_grid_items<float>(int64_t, int);
+template int tma_grid_items<float>(int64_t, int, int);
 template cudaError_t launch_step_multi<float>(const DomainDesc *, int, const int *, const Coef<float> &, bool, bool, int,
-                                            double *, int, int, bool, bool, int *, unsigned long long, int *,
+                                            double *, int, int, bool, bool, int, int *, unsigned long long,
+                                            int *,
                                             cudaStream_t);
 
 }  // namespace ppf

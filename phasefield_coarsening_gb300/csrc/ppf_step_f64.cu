@@ -5,8 +5,9 @@
 
 namespace ppf {
 
-template void step_tile<double>(int *, int *);
-template int make_field_map<double>(const Geom &, const double *, CUtensorMap *);
+template void step_tile<double>(int *, int *, int);
+template int step_tile_shapes<double>();
+template int make_field_map<double>(const Geom &, const double *, CUtensorMap *, int);
 template int tma_grid<double>(const Geom &, int, int *);
 template int tma_grid_for<double>(const Geom &, int, const StepTune &);
 template int64_t tma_items<double>(const Geom &, const StepTune &);

@@ -38,21 +38,34 @@
 
 namespace ppf {
 
-template <typename T>
+// Tile shapes.  TILE 0: FP32 64 x 16 (S = 5: three planes in flight; two
+// CTAs of 256 threads fit an SM), FP64 32 x 16.  TILE 1 (FP32 only): 32 x 32,
+// which fills domains whose x edge is a multiple of 32 but not of 64; four
+// stages (two planes in flight), so that two CTAs still fit an SM.
+template <typename T, int TILE = 0>
 struct TmaCfg;
 template <>
-struct TmaCfg<float> {
-    // S = 5: three planes in flight; two CTAs of 256 threads fit an SM
+struct TmaCfg<float, 0> {
     static constexpr int TX = 64, TY = 16, NT = 256, S = 5, XH = 4;
 };
 template <>
-struct TmaCfg<double> {
+struct TmaCfg<float, 1> {
+    static constexpr int TX = 32, TY = 32, NT = 256, S = 4, XH = 4;
+};
+template <>
+struct TmaCfg<double, 0> {
     static constexpr int TX = 32, TY = 16, NT = 256, S = 4, XH = 2;
 };
+template <>
+struct TmaCfg<double, 1> : TmaCfg<double, 0> {};   // (not instantiated: FP64 has one tile)
 
+// tile shapes per precision
 template <typename T>
+constexpr int kTileShapes = std::is_same<T, float>::value ? 2 : 1;
+
+template <typename T, int TILE = 0>
 struct TmaGeo {
-    using C = TmaCfg<T>;
+    using C = TmaCfg<T, TILE>;
     static constexpr int TX = C::TX, TY = C::TY, NT = C::NT, S = C::S, XH = C::XH;
     static constexpr int BX = TX + 2 * XH, BY = TY + 2;
     static constexpr int BOX = BX * BY;                                   // elements per field box
@@ -65,16 +78,16 @@ struct TmaGeo {
     static_assert(BX * sizeof(T) % 16 == 0 && (XH * sizeof(T)) % 16 == 0, "TMA box alignment");
 };
 
-template <typename T>
+template <typename T, int TILE = 0>
 struct alignas(128) TmaSmem {
-    using G = TmaGeo<T>;
+    using G = TmaGeo<T, TILE>;
     T raw[G::S][3][G::BOX_PAD];   // etaS, etaL, c boxes per stage
     T mm[3][2][G::BOX];           // mu, M of three consecutive planes (MmLay)
     unsigned long long bar[G::S];
 };
 
-template <typename T>
-size_t tma_smem_bytes() { return sizeof(TmaSmem<T>) + 128; }
+template <typename T, int TILE = 0>
+size_t tma_smem_bytes() { return sizeof(TmaSmem<T, TILE>) + 128; }
 
 // ------------------------------------------------------------ PTX glue ----
 
@@ -200,9 +213,9 @@ __device__ __forceinline__ void st2(double *p, V2<double> v) { *reinterpret_cast
 // thread's pair of cells and the pairs beside it in x are one 2-element
 // access each -- then the ring rows -1 and TY as plain rows.  Column c of
 // every row holds x = c - XH.
-template <typename T>
+template <typename T, int TILE = 0>
 struct MmLay {
-    using G = TmaGeo<T>;
+    using G = TmaGeo<T, TILE>;
     static constexpr int H = G::CY / 2;
     static constexpr int TOP = G::TY * G::BX, BOT = TOP + G::BX;
     static_assert(BOT + G::BX == G::BOX, "mu/M plane size");
@@ -410,21 +423,21 @@ __device__ __forceinline__ Item item_at(int item, const Tiles &t1, const ZSplit 
 // SET: the launch's tiles (SET_WHOLE: no per-cell "inside the domain" test;
 // SET_EDGE, SET_ALL: with it; SET_WIDE: with it and 64-bit element offsets,
 // for fields of more than 2^32 elements; the other sets use 32-bit offsets).
-template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL, bool MULTI, int SET>
-__global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
+template <typename T, bool STATS, bool C_ONLY, bool EQ, int ROLL, bool MULTI, int SET, int TILE>
+__global__ void __launch_bounds__(TmaGeo<T, TILE>::NT, 2)
     step_tma_kernel(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapL,
                     const __grid_constant__ CUtensorMap mapC, Geom g1, Coef<T> k, CoefV<T> kv, Fields<T> out1,
                     Tiles t1, ZSplit zs1, double *__restrict__ partials, int *__restrict__ err, unsigned long long limit_ns,
                     int inject_stall, const DomainDesc *__restrict__ table, int ndom, int mitems, int parity,
                     int *__restrict__ sched, int second) {
-    using G = TmaGeo<T>;
+    using G = TmaGeo<T, TILE>;
     constexpr int TX = G::TX, TY = G::TY, S = G::S, XH = G::XH, BX = G::BX, CY = G::CY;
     extern __shared__ __align__(128) unsigned char smem_dyn[];
     // 128-byte alignment by an offset from the shared array itself, so that
     // every derived pointer stays a shared-window pointer (LDS/STS, 32-bit
     // addressing) rather than a generic one
     const uint32_t pad = (128u - (smem_u32(smem_dyn) & 127u)) & 127u;
-    TmaSmem<T> &sm = *reinterpret_cast<TmaSmem<T> *>(smem_dyn + pad);
+    TmaSmem<T, TILE> &sm = *reinterpret_cast<TmaSmem<T, TILE> *>(smem_dyn + pad);
 
     // Programmatic dependent launch (no-ops when the launch does not allow
     // the overlap).  A step is one launch, or two over disjoint tile sets
@@ -458,18 +471,18 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
         if (r < TX) {
             ring_o0 = XH + r;                               // (r, -1)
             ring_o1 = (TY + 1) * BX + XH + r;               // (r, TY)
-            ring_m0 = MmLay<T>::row(-1, XH + r);
-            ring_m1 = MmLay<T>::row(TY, XH + r);
+            ring_m0 = MmLay<T, TILE>::row(-1, XH + r);
+            ring_m1 = MmLay<T, TILE>::row(TY, XH + r);
         } else {
             ring_o0 = (r - TX + 1) * BX + XH - 1;           // (-1, r - TX)
             ring_o1 = (r - TX + 1) * BX + XH + TX;          // (TX, r - TX)
-            ring_m0 = MmLay<T>::row(r - TX, XH - 1);
-            ring_m1 = MmLay<T>::row(r - TX, XH + TX);
+            ring_m0 = MmLay<T, TILE>::row(r - TX, XH - 1);
+            ring_m1 = MmLay<T, TILE>::row(r - TX, XH + TX);
         }
     }
     // the thread's first pair in a mu/M plane, and its rows above and below
-    const int pofs = MmLay<T>::pair((warp / G::WX) * (CY / 2), tx + XH);
-    const int m_above = MmLay<T>::row(ty0 - 1, tx + XH), m_below = MmLay<T>::row(ty0 + CY, tx + XH);
+    const int pofs = MmLay<T, TILE>::pair((warp / G::WX) * (CY / 2), tx + XH);
+    const int m_above = MmLay<T, TILE>::row(ty0 - 1, tx + XH), m_below = MmLay<T, TILE>::row(ty0 + CY, tx + XH);
 
     // increment sums of the statistics step: per thread and work item in the
     // state's precision (packed, one FMA per pair; FP32: at most 2 zc squares
@@ -791,7 +804,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
             if (STATS && !dead) {
                 // the increment sums of each work item, summed later in item order
                 // (the same bits whichever CTA took the item)
-                __shared__ double ired[TmaGeo<T>::NT / 32][3];
+                __shared__ double ired[G::NT / 32][3];
                 __syncthreads();
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
@@ -805,7 +818,7 @@ __global__ void __launch_bounds__(TmaGeo<T>::NT, 2)
                 if (tid == 0)
                     for (int i = 0; i < 3; ++i) {
                         double sv = 0;
-                        for (int w = 0; w < TmaGeo<T>::NT / 32; ++w) sv += ired[w][i];
+                        for (int w = 0; w < G::NT / 32; ++w) sv += ired[w][i];
                         partials[(int64_t)item * 3 + i] = sv;
                     }
             }
@@ -841,9 +854,9 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
     return fn;
 }
 
-template <typename T>
-int make_field_map(const Geom &g, const T *base, CUtensorMap *map) {
-    using G = TmaGeo<T>;
+template <typename T, int TILE>
+static int make_field_map_t(const Geom &g, const T *base, CUtensorMap *map) {
+    using G = TmaGeo<T, TILE>;
     auto enc = get_encode();
     if (!enc) return -1;
     if ((reinterpret_cast<uintptr_t>(base) & 15) || ((g.P * sizeof(T)) & 15)) return -2;
@@ -857,63 +870,93 @@ int make_field_map(const Geom &g, const T *base, CUtensorMap *map) {
     return r == CUDA_SUCCESS ? 0 : -3;
 }
 
-template <typename T, bool ST, bool CO, bool EQ, int R, bool M>
+template <typename T>
+int make_field_map(const Geom &g, const T *base, CUtensorMap *map, int tile) {
+    if (kTileShapes<T> > 1 && tile == 1) return make_field_map_t<T, 1>(g, base, map);
+    return make_field_map_t<T, 0>(g, base, map);
+}
+
+template <typename T, bool ST, bool CO, bool EQ, int R, bool M, int TILE>
 static cudaError_t set_attr1() {
     // (single-domain and ensemble variants are set up, and compiled, in
     // separate translation units)
-    const int sh = (int)tma_smem_bytes<T>();
+    const int sh = (int)tma_smem_bytes<T, TILE>();
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e;
     // (the plane body is unrolled three times only for whole tiles)
-    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, M, SET_WHOLE>, a, sh))) return e;
+    if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, R, M, SET_WHOLE, TILE>, a, sh))) return e;
     if constexpr (R == 1) {
-        if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, 1, M, SET_EDGE>, a, sh)) ||
-            (e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, 1, M, SET_ALL>, a, sh)))
+        if ((e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, 1, M, SET_EDGE, TILE>, a, sh)) ||
+            (e = cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, 1, M, SET_ALL, TILE>, a, sh)))
             return e;
-        if constexpr (!M) return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, 1, false, SET_WIDE>, a, sh);
+        if constexpr (!M) return cudaFuncSetAttribute(step_tma_kernel<T, ST, CO, EQ, 1, false, SET_WIDE, TILE>, a, sh);
     }
     return cudaSuccess;
 }
 
-template <typename T, int R, bool M>
+template <typename T, int R, bool M, int TILE>
 static cudaError_t set_attrs_r() {
     cudaError_t e;
-    if ((e = set_attr1<T, false, false, false, R, M>()) || (e = set_attr1<T, true, false, false, R, M>()) ||
-        (e = set_attr1<T, false, true, false, R, M>()) || (e = set_attr1<T, true, true, false, R, M>()) ||
-        (e = set_attr1<T, false, false, true, R, M>()) || (e = set_attr1<T, true, false, true, R, M>()) ||
-        (e = set_attr1<T, false, true, true, R, M>()) || (e = set_attr1<T, true, true, true, R, M>()))
+    if ((e = set_attr1<T, false, false, false, R, M, TILE>()) || (e = set_attr1<T, true, false, false, R, M, TILE>()) ||
+        (e = set_attr1<T, false, true, false, R, M, TILE>()) || (e = set_attr1<T, true, true, false, R, M, TILE>()) ||
+        (e = set_attr1<T, false, false, true, R, M, TILE>()) || (e = set_attr1<T, true, false, true, R, M, TILE>()) ||
+        (e = set_attr1<T, false, true, true, R, M, TILE>()) || (e = set_attr1<T, true, true, true, R, M, TILE>()))
         return e;
     return cudaSuccess;
 }
 
-// M: the ensemble variants, else the single-domain ones
-template <typename T, bool M>
-static cudaError_t set_attrs() {
-    cudaError_t e = set_attrs_r<T, 1, M>();
-    return e ? e : set_attrs_r<T, 3, M>();
+// CTAs per SM of the step kernels of one tile shape (M: the ensemble
+// variants, else the single-domain ones), with their attributes set first;
+// per device, once.  0 on failure.
+template <typename T, bool M, int TILE>
+static int step_occupancy() {
+    static int occ_of[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    int &occ = occ_of[dev];
+    if (!occ) {
+        if (set_attrs_r<T, 1, M, TILE>() != cudaSuccess || set_attrs_r<T, 3, M, TILE>() != cudaSuccess) return 0;
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 1, M, SET_WHOLE, TILE>,
+                                                          TmaGeo<T, TILE>::NT, tma_smem_bytes<T, TILE>()) != cudaSuccess ||
+            o < 1)
+            o = 1;
+        occ = o;
+    }
+    return occ;
 }
+
+template <typename T, bool M>
+static int step_occupancy(int tile) {
+    if constexpr (kTileShapes<T> > 1)
+        if (tile == 1) return step_occupancy<T, M, 1>();
+    return step_occupancy<T, M, 0>();
+}
+
+template <typename T>
+void step_tile(int *tx, int *ty, int tile) {
+    if (kTileShapes<T> > 1 && tile == 1) {
+        *tx = TmaGeo<T, 1>::TX;
+        *ty = TmaGeo<T, 1>::TY;
+    } else {
+        *tx = TmaGeo<T, 0>::TX;
+        *ty = TmaGeo<T, 0>::TY;
+    }
+}
+
+template <typename T>
+int step_tile_shapes() { return kTileShapes<T>; }
 
 // Launch shape.  Work items are (z chunk, tile) pairs dealt round-robin to
 // a persistent grid of `slots` CTAs (occupancy x SMs).  The chunk length
 // zc is chosen to minimise the busiest CTA's load count -- its planes plus
 // two halo planes per item -- so that the resident CTAs end together;
-// *zc_out receives it.
+// *zc_out receives it (for the first tile shape).
 template <typename T>
 int tma_grid(const Geom &g, int num_sms, int *zc_out) {
-    using G = TmaGeo<T>;
-    // kernel attributes are per device: set them once for each
-    static int occ_of[64];
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
-    int &occ = occ_of[dev];
-    if (!occ) {
-        if (set_attrs<T, false>() != cudaSuccess) return -1;
-        int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 1, false, SET_WHOLE>, G::NT,
-                                                          tma_smem_bytes<T>()) != cudaSuccess || o < 1)
-            o = 1;
-        occ = o;
-    }
+    using G = TmaGeo<T, 0>;
+    const int occ = step_occupancy<T, false>(0);
+    if (occ < 1) return -1;
     const int64_t ntiles = (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY);
     const int64_t slots = (int64_t)occ * num_sms;
     double best_cost = -1;
@@ -922,7 +965,7 @@ int tma_grid(const Geom &g, int num_sms, int *zc_out) {
         const int64_t nc = (g.nz + zc - 1) / zc;
         if (nc > 1 && (nc - 1) * zc >= g.nz) continue;
         const int64_t items = ntiles * nc;
-        if (items > ((int64_t)1 << 30)) continue;
+        if (items > ((int64_t)1 << 29)) continue;
         const int64_t grid = items < slots ? items : slots;
         // items of CTA b: b, b+grid, ...; chunk-major, the last chunk is short
         const int64_t last = g.nz - (nc - 1) * zc;
@@ -960,31 +1003,37 @@ static ZSplit zsplit(const Geom &g, const StepTune &t) {
 }
 
 template <typename T>
+Tiles tiles_of(const Geom &g, int tile) {
+    int tx = 0, ty = 0;
+    step_tile<T>(&tx, &ty, tile);
+    Tiles t;
+    t.ntx = (g.nx + tx - 1) / tx;
+    t.nty = (g.ny + ty - 1) / ty;
+    t.nfx = g.nx / tx;
+    t.nfy = g.ny / ty;
+    return t;
+}
+
+template <typename T>
 int64_t tma_items(const Geom &g, const StepTune &t) {
-    using G = TmaGeo<T>;
     const ZSplit s = zsplit(g, t);
     const int64_t chunks = s.n1 + (g.nz - s.n1 * s.zc + s.zc2 - 1) / s.zc2;
-    return (int64_t)((g.nx + G::TX - 1) / G::TX) * ((g.ny + G::TY - 1) / G::TY) * chunks;
+    const Tiles tl = tiles_of<T>(g, t.tile);
+    return (int64_t)tl.ntx * tl.nty * chunks;
 }
 
 template <typename T>
 int tma_grid_for(const Geom &g, int num_sms, const StepTune &t) {
-    using G = TmaGeo<T>;
-    int dummy = 0;
-    if (tma_grid<T>(g, num_sms, &dummy) < 1) return -1;    // attributes + occupancy
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, step_tma_kernel<T, false, false, true, 1, false, SET_WHOLE>, G::NT,
-                                                      tma_smem_bytes<T>()) != cudaSuccess || occ < 1)
-        occ = 1;
+    const int occ = step_occupancy<T, false>(t.tile);
+    if (occ < 1) return -1;
     const int64_t items = tma_items<T>(g, t);
     const int64_t slots = (int64_t)occ * num_sms;
-    if (items > ((int64_t)1 << 30)) return -1;
+    if (items > ((int64_t)1 << 29)) return -1;
     return (int)(items < slots ? items : slots);
 }
 
-// A launch of the single-domain step; with `pdl` the launch allows
-// programmatic dependent launch (the kernel's griddepcontrol.wait keeps the
-// stream order for every global memory access).
+// A launch of the step; with `pdl` the launch allows programmatic dependent
+// launch (see the kernel's griddepcontrol use).
 template <typename... KArgs, typename... Args>
 static void launch_step_ex(bool pdl, void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
                            Args... args) {
@@ -1002,32 +1051,21 @@ static void launch_step_ex(bool pdl, void (*kern)(KArgs...), int grid, int block
     (void)cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
-template <typename T>
-Tiles tiles_of(const Geom &g) {
-    using G = TmaGeo<T>;
-    Tiles t;
-    t.ntx = (g.nx + G::TX - 1) / G::TX;
-    t.nty = (g.ny + G::TY - 1) / G::TY;
-    t.nfx = g.nx / G::TX;
-    t.nfy = g.ny / G::TY;
-    return t;
-}
-
 // One launch of the single-domain step over the items of one tile set.
-template <typename T, int R, int SET>
+template <typename T, int R, int SET, int TILE>
 static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only, bool eqA,
                      double *partials, const StepTune &tune, int items, int *err, unsigned long long limit_ns,
                      int inject_stall, int *sched, int second, cudaStream_t s) {
-    using G = TmaGeo<T>;
-    const size_t sh = tma_smem_bytes<T>();
+    using G = TmaGeo<T, TILE>;
+    const size_t sh = tma_smem_bytes<T, TILE>();
     const bool st = partials != nullptr;
     const CoefV<T> kv = make_coefv(k);
     const DomainDesc *no_table = nullptr;
     const ZSplit zs = zsplit(g, tune);
-    const Tiles t = tiles_of<T>(g);
+    const Tiles t = tiles_of<T>(g, TILE);
     const int grid = items < tune.grid ? items : tune.grid;
 #define PPF_LAUNCH(ST, CO, EQ)                                                                                        \
-    launch_step_ex(tune.pdl != 0, step_tma_kernel<T, ST, CO, EQ, R, false, SET>, grid, G::NT, sh, s, maps[0],         \
+    launch_step_ex(tune.pdl != 0, step_tma_kernel<T, ST, CO, EQ, R, false, SET, TILE>, grid, G::NT, sh, s, maps[0],   \
                    maps[1], maps[2], g, k, kv, out, t, zs, partials, err, limit_ns, inject_stall, no_table, 0, items,   \
                    0, tune.sched ? sched : nullptr, second)
     if (eqA) {
@@ -1040,52 +1078,67 @@ static void launch_r(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, F
 #undef PPF_LAUNCH
 }
 
-template <typename T, int R>
+template <typename T, int R, int TILE>
 static void launch_sets(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
                         bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
                         int inject_stall, int *sched, cudaStream_t s) {
-    const Tiles t = tiles_of<T>(g);
+    const Tiles t = tiles_of<T>(g, TILE);
     const int64_t chunks = tma_items<T>(g, tune) / ((int64_t)t.ntx * t.nty);
     const int na = (int)(chunks * t.ntx * t.nty);
     if (g.total > ((int64_t)1 << 32)) {        // 64-bit offsets: one launch over every tile
-        launch_r<T, 1, SET_WIDE>(g, k, maps, out, c_only, eqA, partials, tune, na, err, limit_ns, inject_stall, sched,
-                                 0, s);
+        launch_r<T, 1, SET_WIDE, TILE>(g, k, maps, out, c_only, eqA, partials, tune, na, err, limit_ns, inject_stall,
+                                       sched, 0, s);
         return;
     }
     const int nw = (int)(chunks * tiles_in_set(t, SET_WHOLE)), ne = (int)(chunks * tiles_in_set(t, SET_EDGE));
     if (ne == 0) {                             // every tile inside the domain
-        launch_r<T, R, SET_WHOLE>(g, k, maps, out, c_only, eqA, partials, tune, nw, err, limit_ns, inject_stall, sched,
-                                  0, s);
+        launch_r<T, R, SET_WHOLE, TILE>(g, k, maps, out, c_only, eqA, partials, tune, nw, err, limit_ns, inject_stall,
+                                        sched, 0, s);
         return;
     }
     if (!tune.split || nw == 0) {              // one launch over every tile
-        launch_r<T, 1, SET_ALL>(g, k, maps, out, c_only, eqA, partials, tune, na, err, limit_ns, inject_stall, sched,
-                                0, s);
+        launch_r<T, 1, SET_ALL, TILE>(g, k, maps, out, c_only, eqA, partials, tune, na, err, limit_ns, inject_stall,
+                                      sched, 0, s);
         return;
     }
     // the whole tiles, then the edge tiles (their increment sums follow the
     // whole tiles' in `partials`; their own scheduler pair, since the two
     // launches overlap)
-    launch_r<T, R, SET_WHOLE>(g, k, maps, out, c_only, eqA, partials, tune, nw, err, limit_ns, inject_stall, sched, 0, s);
-    launch_r<T, 1, SET_EDGE>(g, k, maps, out, c_only, eqA, partials ? partials + 3 * (int64_t)nw : nullptr, tune, ne,
-                             err, limit_ns, 0, sched ? sched + 2 : nullptr, 1, s);
+    launch_r<T, R, SET_WHOLE, TILE>(g, k, maps, out, c_only, eqA, partials, tune, nw, err, limit_ns, inject_stall,
+                                    sched, 0, s);
+    launch_r<T, 1, SET_EDGE, TILE>(g, k, maps, out, c_only, eqA, partials ? partials + 3 * (int64_t)nw : nullptr, tune,
+                                   ne, err, limit_ns, 0, sched ? sched + 2 : nullptr, 1, s);
+}
+
+template <typename T, int TILE>
+static void launch_tile(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
+                        bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
+                        int inject_stall, int *sched, cudaStream_t s) {
+    if (tune.roll == 1)
+        launch_sets<T, 1, TILE>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
+    else
+        launch_sets<T, 3, TILE>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
 }
 
 template <typename T>
 cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *maps, Fields<T> out, bool c_only,
                             bool eqA, double *partials, const StepTune &tune, int *err, unsigned long long limit_ns,
                             int inject_stall, int *sched, cudaStream_t s) {
-    if (tune.roll == 1) launch_sets<T, 1>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
-    else launch_sets<T, 3>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
+    if constexpr (kTileShapes<T> > 1)
+        if (tune.tile == 1) {
+            launch_tile<T, 1>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
+            return cudaGetLastError();
+        }
+    launch_tile<T, 0>(g, k, maps, out, c_only, eqA, partials, tune, err, limit_ns, inject_stall, sched, s);
     return cudaGetLastError();
 }
 
-template <typename T, int R, int SET>
+template <typename T, int R, int SET, int TILE>
 static void launch_multi_r(const DomainDesc *table, int ndom, int items, const Coef<T> &k, bool c_only, bool eqA,
                            int parity, double *partials, int grid, int *err, unsigned long long limit_ns,
                            int *sched, bool pdl, int second, cudaStream_t s) {
-    using G = TmaGeo<T>;
-    const size_t sh = tma_smem_bytes<T>();
+    using G = TmaGeo<T, TILE>;
+    const size_t sh = tma_smem_bytes<T, TILE>();
     const bool st = partials != nullptr;
     CUtensorMap none;
     memset(&none, 0, sizeof none);
@@ -1097,8 +1150,8 @@ static void launch_multi_r(const DomainDesc *table, int ndom, int items, const C
     const Tiles t0 = {1, 1, 1, 1};
     if (items < grid) grid = items;
 #define PPF_LAUNCH(ST, CO, EQ)                                                                                       \
-    launch_step_ex(pdl, step_tma_kernel<T, ST, CO, EQ, R, true, SET>, grid, G::NT, sh, s, none, none, none, g0, k, kv, \
-                   o0, t0, z1, partials, err, limit_ns, 0, table, ndom, items, parity, sched, second)
+    launch_step_ex(pdl, step_tma_kernel<T, ST, CO, EQ, R, true, SET, TILE>, grid, G::NT, sh, s, none, none, none, g0, \
+                   k, kv, o0, t0, z1, partials, err, limit_ns, 0, table, ndom, items, parity, sched, second)
     if (eqA) {
         if (!c_only) { if (st) PPF_LAUNCH(true, false, true); else PPF_LAUNCH(false, false, true); }
         else { if (st) PPF_LAUNCH(true, true, true); else PPF_LAUNCH(false, true, true); }
@@ -1109,52 +1162,58 @@ static void launch_multi_r(const DomainDesc *table, int ndom, int items, const C
 #undef PPF_LAUNCH
 }
 
-template <typename T>
-cudaError_t launch_step_multi(const DomainDesc *table, int ndom, const int *items, const Coef<T> &k, bool c_only,
+template <typename T, int TILE>
+static void launch_multi_tile(const DomainDesc *table, int ndom, const int *items, const Coef<T> &k, bool c_only,
                               bool eqA, int parity, double *partials, int grid, int roll, bool pdl, bool split,
                               int *err, unsigned long long limit_ns, int *sched, cudaStream_t s) {
     const int nw = items[1], ne = items[0], na = items[2];
     if (ne == 0) {                             // every tile of every domain inside its domain
-        if (roll == 1) launch_multi_r<T, 1, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
-        else launch_multi_r<T, 3, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
-        return cudaGetLastError();
+        if (roll == 1)
+            launch_multi_r<T, 1, SET_WHOLE, TILE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns,
+                                                  sched, pdl, 0, s);
+        else
+            launch_multi_r<T, 3, SET_WHOLE, TILE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns,
+                                                  sched, pdl, 0, s);
+        return;
     }
     if (!split || nw == 0) {                   // one launch over every tile
-        launch_multi_r<T, 1, SET_ALL>(table, ndom, na, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
-        return cudaGetLastError();
+        launch_multi_r<T, 1, SET_ALL, TILE>(table, ndom, na, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched,
+                                            pdl, 0, s);
+        return;
     }
     // the whole tiles of every domain, then the edge tiles (their increment
     // sums follow the whole tiles' in `partials`; their own scheduler pair,
     // since the two launches overlap)
-    if (roll == 1) launch_multi_r<T, 1, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
-    else launch_multi_r<T, 3, SET_WHOLE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns, sched, pdl, 0, s);
-    launch_multi_r<T, 1, SET_EDGE>(table, ndom, ne, k, c_only, eqA, parity, partials ? partials + 3 * (int64_t)nw : nullptr,
-                                   grid, err, limit_ns, sched ? sched + 2 : nullptr, pdl, 1, s);
+    if (roll == 1)
+        launch_multi_r<T, 1, SET_WHOLE, TILE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns,
+                                              sched, pdl, 0, s);
+    else
+        launch_multi_r<T, 3, SET_WHOLE, TILE>(table, ndom, nw, k, c_only, eqA, parity, partials, grid, err, limit_ns,
+                                              sched, pdl, 0, s);
+    launch_multi_r<T, 1, SET_EDGE, TILE>(table, ndom, ne, k, c_only, eqA, parity,
+                                         partials ? partials + 3 * (int64_t)nw : nullptr, grid, err, limit_ns,
+                                         sched ? sched + 2 : nullptr, pdl, 1, s);
+}
+
+template <typename T>
+cudaError_t launch_step_multi(const DomainDesc *table, int ndom, const int *items, const Coef<T> &k, bool c_only,
+                              bool eqA, int parity, double *partials, int grid, int roll, bool pdl, bool split,
+                              int tile, int *err, unsigned long long limit_ns, int *sched, cudaStream_t s) {
+    if constexpr (kTileShapes<T> > 1)
+        if (tile == 1) {
+            launch_multi_tile<T, 1>(table, ndom, items, k, c_only, eqA, parity, partials, grid, roll, pdl, split, err,
+                                    limit_ns, sched, s);
+            return cudaGetLastError();
+        }
+    launch_multi_tile<T, 0>(table, ndom, items, k, c_only, eqA, parity, partials, grid, roll, pdl, split, err, limit_ns,
+                            sched, s);
     return cudaGetLastError();
 }
 
 template <typename T>
-void step_tile(int *tx, int *ty) {
-    *tx = TmaGeo<T>::TX;
-    *ty = TmaGeo<T>::TY;
-}
-
-template <typename T>
-int tma_grid_items(int64_t items, int num_sms) {
-    // kernel attributes of the ensemble variants are per device: set them once for each
-    static int occ_of[64];
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
-    int &occ = occ_of[dev];
-    if (!occ) {
-        if (set_attrs<T, true>() != cudaSuccess) return -1;
-        int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, step_tma_kernel<T, false, false, true, 1, true, SET_WHOLE>,
-                                                          TmaGeo<T>::NT, tma_smem_bytes<T>()) != cudaSuccess ||
-            o < 1)
-            o = 1;
-        occ = o;
-    }
+int tma_grid_items(int64_t items, int num_sms, int tile) {
+    const int occ = step_occupancy<T, true>(tile);
+    if (occ < 1) return -1;
     const int64_t slots = (int64_t)occ * num_sms;
     return (int)(items < slots ? items : slots);
 }

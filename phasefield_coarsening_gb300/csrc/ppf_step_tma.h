@@ -31,15 +31,16 @@ struct StepTune {
     int zc2;    // > 0 (and < zc): the top `tail` planes are cut into chunks of zc2
     int tail;
     int split;  // 1: whole tiles and edge tiles as two overlapping launches; 0: one launch
+    int tile;   // tile shape (step_tile); FP32 has two, FP64 one
 };
 
 // Tensor map of one padded field (3-D: x pitch, ny+2 rows, nz+2 planes)
-// with the kernel's box; 0 on success.
+// with the box of tile shape `tile`; 0 on success.
 template <typename T>
-int make_field_map(const Geom &g, const T *base, CUtensorMap *map);
+int make_field_map(const Geom &g, const T *base, CUtensorMap *map, int tile);
 
 // Persistent grid size (occupancy x SMs, capped by the work) and the z
-// chunk length of a work item; < 0 on error.
+// chunk length of a work item, for the first tile shape; < 0 on error.
 template <typename T>
 int tma_grid(const Geom &g, int num_sms, int *zc);
 
@@ -64,13 +65,17 @@ cudaError_t launch_step_tma(const Geom &g, const Coef<T> &k, const CUtensorMap *
 template <typename T>
 int64_t tma_items(const Geom &g, const StepTune &t);
 
-// Tiles of the fused step (x, y), for sizing ensemble work items.
+// Tile (x, y) of tile shape `tile` of the fused step, and the number of
+// tile shapes of the precision.
 template <typename T>
-void step_tile(int *tx, int *ty);
+void step_tile(int *tx, int *ty, int tile);
+template <typename T>
+int step_tile_shapes();
 
-// Persistent grid for `items` work items (occupancy x SMs, capped).
+// Persistent grid of the ensemble step for `items` work items of tile
+// shape `tile` (occupancy x SMs, capped).
 template <typename T>
-int tma_grid_items(int64_t items, int num_sms);
+int tma_grid_items(int64_t items, int num_sms, int tile);
 
 // One fused step of every domain of an ensemble: reads buffer `parity` of
 // each domain and writes buffer 1-parity, as one launch over every tile
@@ -81,6 +86,6 @@ int tma_grid_items(int64_t items, int num_sms);
 template <typename T>
 cudaError_t launch_step_multi(const DomainDesc *table, int ndom, const int *items, const Coef<T> &k, bool c_only,
                               bool eqA, int parity, double *partials, int grid, int roll, bool pdl, bool split,
-                              int *err, unsigned long long limit_ns, int *sched, cudaStream_t s);
+                              int tile, int *err, unsigned long long limit_ns, int *sched, cudaStream_t s);
 
 }  // namespace ppf

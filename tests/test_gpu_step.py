@@ -268,16 +268,19 @@ def test_launch_choices_are_bit_identical(precision):
     shape = (40, 35, 70)
     st = smooth_state(shape, seed=12)
     ref, inc_of = None, {}
-    # (the grid has whole tiles and edge tiles in x and y: one launch over
-    # every tile, or two overlapping launches, split = 0 / 1)
-    for zc, roll, pdl, sched, zc2, tail, split in [
-            (None,) * 7, (1, 3, 1, 1, 0, 0, 1), (1, 1, 0, 0, 0, 0, 0), (7, 1, 0, 0, 0, 0, 1), (7, 3, 1, 1, 0, 0, 0),
-            (40, 3, 0, 1, 0, 0, 1), (40, 1, 1, 0, 0, 0, 0), (13, 1, 1, 0, 0, 0, 1), (13, 3, 0, 1, 0, 0, 0),
-            (2, 1, 1, 1, 0, 0, 0), (12, 3, 1, 1, 4, 10, 1), (12, 1, 1, 0, 4, 10, 0), (9, 1, 0, 1, 2, 31, 1),
-            (16, 3, 1, 1, 5, 40, 0)]:
+    # (the grid has whole tiles and edge tiles in x and y with either tile
+    # shape: one launch over every tile, or two overlapping launches,
+    # split = 0 / 1; the 32 x 32 tile shape, tile = 1, is FP32's only)
+    t1 = 1 if precision == "f32" else 0
+    for zc, roll, pdl, sched, zc2, tail, split, tile in [
+            (None,) * 8, (1, 3, 1, 1, 0, 0, 1, 0), (1, 1, 0, 0, 0, 0, 0, 0), (7, 1, 0, 0, 0, 0, 1, 0),
+            (7, 3, 1, 1, 0, 0, 0, 0), (40, 3, 0, 1, 0, 0, 1, 0), (40, 1, 1, 0, 0, 0, 0, 0), (13, 1, 1, 0, 0, 0, 1, 0),
+            (13, 3, 0, 1, 0, 0, 0, 0), (2, 1, 1, 1, 0, 0, 0, 0), (12, 3, 1, 1, 4, 10, 1, 0), (12, 1, 1, 0, 4, 10, 0, 0),
+            (9, 1, 0, 1, 2, 31, 1, 0), (16, 3, 1, 1, 5, 40, 0, 0), (7, 3, 1, 1, 0, 0, 1, t1), (7, 1, 0, 0, 0, 0, 0, t1),
+            (13, 3, 1, 1, 5, 20, 1, t1), (40, 1, 1, 1, 0, 0, 0, t1)]:
         with ppf.Simulation(shape, bc=1, precision=precision) as s:
             if zc is not None:
-                s.set_tune(zc, roll, pdl, sched, zc2, tail, split)
+                s.set_tune(zc, roll, pdl, sched, zc2, tail, split, tile)
             s.upload(*st)
             for _ in range(3):            # several launches: every launch resets the counter
                 s.step(2)
@@ -288,12 +291,20 @@ def test_launch_choices_are_bit_identical(precision):
             ref, ref_inc = out, inc
         else:
             for a, b in zip(out, ref):
-                assert np.array_equal(a, b), (zc, roll, pdl, sched, zc2, tail, split)
+                assert np.array_equal(a, b), (zc, roll, pdl, sched, zc2, tail, split, tile)
             np.testing.assert_allclose(inc, ref_inc, rtol=1e-13 if precision == "f64" else 1e-5)
-            key = (zc, zc2, tail, split)          # the same work items, summed in the same order
+            key = (zc, zc2, tail, split, tile)    # the same work items, summed in the same order
             if key in inc_of:
-                assert inc == inc_of[key], (zc, roll, pdl, sched, zc2, tail, split)
+                assert inc == inc_of[key], (zc, roll, pdl, sched, zc2, tail, split, tile)
             inc_of[key] = inc
+
+
+def test_fp64_has_one_tile_shape():
+    with ppf.Simulation((8, 8, 8), precision="f64") as s:
+        with pytest.raises(ppf.PPFError):
+            s.set_tune(4, 1, 1, 1, 0, 0, 1, 1)
+        s.set_tune(4, 1, 1, 1, 0, 0, 1, 0)
+        assert s.get_tune()["tile"] == 0
 
 
 def test_autotune_keeps_state_and_picks_a_valid_choice():

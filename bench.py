@@ -52,6 +52,8 @@ WORKLOAD = "spheres256_lognormal5_vf30"
 DT_LIMIT = 1.0 / (6.0 * 1e-14)
 DT = 0.8 * DT_LIMIT
 INNER = 100
+# host threads / contexts (or ensembles) that take turns in the end-to-end measurements
+E2E_CONTEXTS = 3
 ALG_BYTES_F32 = 24          # read etaS, etaL, c + write 3, float
 
 
@@ -312,17 +314,21 @@ def run_ours(args):
 
     # e2e through the C-ABI with pinned host buffers.  Every bench step
     # uploads its input from pinned host memory, steps, reduces and downloads
-    # its result.  Two contexts on two streams, each driven by its own host
-    # thread (the C-ABI's one-context-per-thread model; the calls release
-    # the GIL), take alternate bench steps, so that one context's host-link
-    # copies overlap the other's stepping.
-    sim2 = ppf.Simulation(shape, ppf.params_default(dt=DT), bc="periodic", precision="f32")
-    stream2 = torch.cuda.Stream()
-    sim2.set_stream(stream2.cuda_stream)
-    sim2.set_tune(tune["zc"], tune["roll"], tune["pdl"], tune["sched"], tune["zc2"], tune["tail"], tune["split"],
-                  tune["tile"])
+    # its result.  E2E_CONTEXTS contexts on their own streams, each driven by
+    # its own host thread (the C-ABI's one-context-per-thread model; the calls
+    # release the GIL), take turns at the bench steps, so that the host-link
+    # copies of some overlap the others' stepping (measured on a GB300: 133,
+    # 171 and 202 GLUPS with one, two and three contexts, 215 device-only).
+    extra, streams = [], []
+    for _ in range(E2E_CONTEXTS - 1):
+        sx = ppf.Simulation(shape, ppf.params_default(dt=DT), bc="periodic", precision="f32")
+        streams.append(torch.cuda.Stream())
+        sx.set_stream(streams[-1].cuda_stream)
+        sx.set_tune(tune["zc"], tune["roll"], tune["pdl"], tune["sched"], tune["zc2"], tune["tail"], tune["split"],
+                    tune["tile"])
+        extra.append(sx)
     host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (eS, eL, c)]
-    outh = [[torch.empty(shape, dtype=torch.float64).pin_memory() for _ in range(3)] for _ in range(2)]
+    outh = [[torch.empty(shape, dtype=torch.float64).pin_memory() for _ in range(3)] for _ in range(E2E_CONTEXTS)]
     ptr_in = [h.data_ptr() for h in host]
 
     def e2e_worker(s, outp, n):
@@ -334,20 +340,22 @@ def run_ours(args):
             s.download_into(*ptr_out)
 
     def e2e_run(n):
-        ths = [threading.Thread(target=e2e_worker, args=(s, o, (n + 1 - i) // 2))
-               for i, (s, o) in enumerate(zip((sim, sim2), outh))]
+        k = E2E_CONTEXTS
+        ths = [threading.Thread(target=e2e_worker, args=(s, o, (n + k - 1 - i) // k))
+               for i, (s, o) in enumerate(zip([sim] + extra, outh))]
         for t in ths:
             t.start()
         for t in ths:
             t.join()
 
-    e2e_run(max(2, args.warmup))
+    e2e_run(max(E2E_CONTEXTS, args.warmup))
     torch.cuda.synchronize()
     w0 = time.perf_counter()
     e2e_run(args.steps)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - w0
-    sim2.close()
+    for sx in extra:
+        sx.close()
     e2e_s = max_over_ranks(e2e_s)
     e2e_value = job_glups(world, cells, INNER * args.steps, e2e_s)
 
@@ -373,8 +381,8 @@ def run_ours(args):
             "e2e": {"value": round(e2e_value, 3), "unit": "GLUPS", "h2d_bytes_per_step": 3 * cells * 8,
                     "d2h_bytes_per_step": 3 * cells * 8 + 8 * 8,
                     "how": "ppf_upload (pinned float64 host arrays) + 100 ppf_step + ppf_reduce + ppf_download "
-                           "per bench step; two contexts on two streams, one host thread each, take alternate "
-                           "bench steps so that copies overlap stepping; wall clock over all steps"},
+                           f"per bench step; {E2E_CONTEXTS} contexts on their own streams, one host thread each, take "
+                           "turns at the bench steps so that copies overlap stepping; wall clock over all steps"},
             "gpu_launches": args.steps * (INNER + 1 + 2),
             "clocks": clk,
             "final_stats": {k: stats[k] for k in ("mass", "solid", "free_energy", "nonfinite")},
@@ -498,15 +506,19 @@ def run_ensemble(args):
     clk = clocks.stop()
 
     # e2e through the C-ABI: every bench step uploads all domains from pinned
-    # host memory, steps, and downloads all domains.  Two ensembles, one host
-    # thread each, take alternate bench steps so that one's host-link copies
-    # overlap the other's stepping (as in the single-domain line).
-    ens2 = ppf.Ensemble(shapes, prm, bc="periodic", precision="f32")
-    ens2.set_tune(tune["zc"], tune["roll"], tune["sched"], tune["pdl"], tune["split"], tune["tile"])
+    # host memory, steps, and downloads all domains.  E2E_CONTEXTS ensembles,
+    # one host thread each, take turns at the bench steps so that the
+    # host-link copies of some overlap the others' stepping (as in the
+    # single-domain line).
+    extra = []
+    for _ in range(E2E_CONTEXTS - 1):
+        ex = ppf.Ensemble(shapes, prm, bc="periodic", precision="f32")
+        ex.set_tune(tune["zc"], tune["roll"], tune["sched"], tune["pdl"], tune["split"], tune["tile"])
+        extra.append(ex)
     L = ppf.lib()
     pin_in = [[torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in d[:3]] for d in doms]
     pin_out = [[[torch.empty(s, dtype=torch.float64).pin_memory() for _ in range(3)] for s in shapes]
-               for _ in range(2)]
+               for _ in range(E2E_CONTEXTS)]
 
     def e2e_worker(e, outs, n):
         for _ in range(n):
@@ -518,18 +530,20 @@ def run_ensemble(args):
             e.sync()
 
     def e2e_run(n):
-        ths = [threading.Thread(target=e2e_worker, args=(e, o, (n + 1 - i) // 2))
-               for i, (e, o) in enumerate(zip((ens, ens2), pin_out))]
+        k = E2E_CONTEXTS
+        ths = [threading.Thread(target=e2e_worker, args=(e, o, (n + k - 1 - i) // k))
+               for i, (e, o) in enumerate(zip([ens] + extra, pin_out))]
         for t in ths:
             t.start()
         for t in ths:
             t.join()
 
-    e2e_run(max(2, args.warmup))
+    e2e_run(max(E2E_CONTEXTS, args.warmup))
     w0 = time.perf_counter()
     e2e_run(args.steps)
     e2e_s = max_over_ranks(time.perf_counter() - w0)
-    ens2.close()
+    for ex in extra:
+        ex.close()
     e2e_value = job_glups(world, cells, INNER * args.steps, e2e_s)
     if rank == 0:
         line = {
@@ -547,8 +561,9 @@ def run_ensemble(args):
             "e2e": {"value": round(e2e_value, 3), "unit": "GLUPS", "h2d_bytes_per_step": 3 * cells * 8,
                     "d2h_bytes_per_step": 3 * cells * 8,
                     "how": "ppf_ensemble_upload of every domain (pinned float64 host arrays) + 100 steps + "
-                           "ppf_ensemble_download of every domain per bench step; two ensembles, one host thread "
-                           "each, take alternate bench steps so that copies overlap stepping; wall clock"},
+                           "ppf_ensemble_download of every domain per bench step; E2E_CONTEXTS ensembles, one host "
+                           "thread each, take turns at the bench steps so that copies overlap stepping; wall clock"
+                           .replace("E2E_CONTEXTS", str(E2E_CONTEXTS))},
             "gpu_launches": args.steps * INNER,
             "clocks": clk,
         }

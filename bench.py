@@ -52,8 +52,11 @@ WORKLOAD = "spheres256_lognormal5_vf30"
 DT_LIMIT = 1.0 / (6.0 * 1e-14)
 DT = 0.8 * DT_LIMIT
 INNER = 100
-# host threads / contexts (or ensembles) that take turns in the end-to-end measurements
+# host threads / contexts that take turns in the end-to-end measurement,
+# and ensembles in the ensemble's (measured best: 3 contexts 202 GLUPS, 2
+# ensembles with the batched upload/download 130 against 110 with 3)
 E2E_CONTEXTS = 3
+ENS_E2E_ENSEMBLES = 2
 ALG_BYTES_F32 = 24          # read etaS, etaL, c + write 3, float
 
 
@@ -506,31 +509,31 @@ def run_ensemble(args):
     clk = clocks.stop()
 
     # e2e through the C-ABI: every bench step uploads all domains from pinned
-    # host memory, steps, and downloads all domains.  E2E_CONTEXTS ensembles,
+    # host memory, steps, and downloads all domains.  ENS_E2E_ENSEMBLES ensembles,
     # one host thread each, take turns at the bench steps so that the
     # host-link copies of some overlap the others' stepping (as in the
     # single-domain line).
     extra = []
-    for _ in range(E2E_CONTEXTS - 1):
+    for _ in range(ENS_E2E_ENSEMBLES - 1):
         ex = ppf.Ensemble(shapes, prm, bc="periodic", precision="f32")
         ex.set_tune(tune["zc"], tune["roll"], tune["sched"], tune["pdl"], tune["split"], tune["tile"])
         extra.append(ex)
-    L = ppf.lib()
     pin_in = [[torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in d[:3]] for d in doms]
     pin_out = [[[torch.empty(s, dtype=torch.float64).pin_memory() for _ in range(3)] for s in shapes]
-               for _ in range(E2E_CONTEXTS)]
+               for _ in range(ENS_E2E_ENSEMBLES)]
+
+    ptr_in = [[t.data_ptr() for t in arrs] for arrs in pin_in]
 
     def e2e_worker(e, outs, n):
+        ptr_out = [[t.data_ptr() for t in arrs] for arrs in outs]
         for _ in range(n):
-            for i, arrs in enumerate(pin_in):
-                ppf._check(L.ppf_ensemble_upload(e.handle, i, *[t.data_ptr() for t in arrs]))
+            e.upload_from_all(ptr_in)          # ppf_ensemble_upload_all
             e.step(INNER)
-            for i, arrs in enumerate(outs):
-                ppf._check(L.ppf_ensemble_download(e.handle, i, *[t.data_ptr() for t in arrs]))
+            e.download_into_all(ptr_out)       # ppf_ensemble_download_all
             e.sync()
 
     def e2e_run(n):
-        k = E2E_CONTEXTS
+        k = ENS_E2E_ENSEMBLES
         ths = [threading.Thread(target=e2e_worker, args=(e, o, (n + k - 1 - i) // k))
                for i, (e, o) in enumerate(zip([ens] + extra, pin_out))]
         for t in ths:
@@ -538,7 +541,7 @@ def run_ensemble(args):
         for t in ths:
             t.join()
 
-    e2e_run(max(E2E_CONTEXTS, args.warmup))
+    e2e_run(max(ENS_E2E_ENSEMBLES, args.warmup))
     w0 = time.perf_counter()
     e2e_run(args.steps)
     e2e_s = max_over_ranks(time.perf_counter() - w0)
@@ -560,10 +563,10 @@ def run_ensemble(args):
             "sequential_equals_ensemble": sec["sequential_equals_ensemble"],
             "e2e": {"value": round(e2e_value, 3), "unit": "GLUPS", "h2d_bytes_per_step": 3 * cells * 8,
                     "d2h_bytes_per_step": 3 * cells * 8,
-                    "how": "ppf_ensemble_upload of every domain (pinned float64 host arrays) + 100 steps + "
-                           "ppf_ensemble_download of every domain per bench step; E2E_CONTEXTS ensembles, one host "
+                    "how": "ppf_ensemble_upload_all (pinned float64 host arrays of every domain) + 100 steps + "
+                           "ppf_ensemble_download_all per bench step; ENS_E2E_ENSEMBLES ensembles, one host "
                            "thread each, take turns at the bench steps so that copies overlap stepping; wall clock"
-                           .replace("E2E_CONTEXTS", str(E2E_CONTEXTS))},
+                           .replace("ENS_E2E_ENSEMBLES", str(ENS_E2E_ENSEMBLES))},
             "gpu_launches": args.steps * INNER,
             "clocks": clk,
         }

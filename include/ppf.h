@@ -256,6 +256,15 @@ int ppf_ensemble_destroy(ppf_ensemble *ens);
 int ppf_ensemble_domain(ppf_ensemble *ens, int d, ppf_ctx **ctx);
 int ppf_ensemble_upload(ppf_ensemble *ens, int d, const double *etaS, const double *etaL, const double *c);
 int ppf_ensemble_download(ppf_ensemble *ens, int d, double *etaS, double *etaL, double *c);
+/* Every domain in one call: arrays of n host pointers per field (domain d's
+ * compact [z][y][x] float64 arrays).  The copies of all domains are issued
+ * first and one conversion launch covers them all, so that a caller that
+ * streams ensembles through host memory while other ensembles step on the
+ * same device waits for a free SM slot once per call, not once per domain.
+ * Same results as n calls of ppf_ensemble_upload / ppf_ensemble_download. */
+int ppf_ensemble_upload_all(ppf_ensemble *ens, const double *const *etaS, const double *const *etaL,
+                            const double *const *c);
+int ppf_ensemble_download_all(ppf_ensemble *ens, double *const *etaS, double *const *etaL, double *const *c);
 /* nsteps full steps of every domain (all domains need an uploaded state);
  * the last step's increment sums go to each domain's ppf_reduce. */
 int ppf_ensemble_step(ppf_ensemble *ens, int64_t nsteps);

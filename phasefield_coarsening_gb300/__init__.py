@@ -29,7 +29,8 @@ EXPORTS = (
     "ppf_upload", "ppf_download", "ppf_upload_device", "ppf_download_device", "ppf_step", "ppf_step_c_only",
     "ppf_reduce", "ppf_sync", "ppf_set_wait_limit", "ppf_debug_inject", "ppf_get_tune", "ppf_set_tune",
     "ppf_autotune", "ppf_observe_noalloc", "ppf_particles", "ppf_ensemble_create", "ppf_ensemble_destroy",
-    "ppf_ensemble_domain", "ppf_ensemble_upload", "ppf_ensemble_download", "ppf_ensemble_step",
+    "ppf_ensemble_domain", "ppf_ensemble_upload", "ppf_ensemble_download", "ppf_ensemble_upload_all",
+    "ppf_ensemble_download_all", "ppf_ensemble_step",
     "ppf_ensemble_reduce", "ppf_ensemble_sync", "ppf_ensemble_get_tune", "ppf_ensemble_set_tune",
     "ppf_ensemble_autotune", "ppf_slabs_plan", "ppf_slabs_create", "ppf_slabs_destroy", "ppf_slabs_upload",
     "ppf_slabs_download", "ppf_slabs_step", "ppf_slabs_reduce", "ppf_slabs_sync", "ppf_mass_project", "ppf_copy_state", "ppf_surrogate_config_default",
@@ -144,6 +145,8 @@ def lib() -> ctypes.CDLL:
         L.ppf_ensemble_domain.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
         for n in ("ppf_ensemble_upload", "ppf_ensemble_download"):
             getattr(L, n).argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
+        for n in ("ppf_ensemble_upload_all", "ppf_ensemble_download_all"):
+            getattr(L, n).argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_void_p)] * 3
         L.ppf_ensemble_step.argtypes = [ctypes.c_void_p, ctypes.c_int64]
         L.ppf_ensemble_reduce.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Stats)]
         L.ppf_ensemble_get_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Tune)]
@@ -450,6 +453,37 @@ class Ensemble:
         out = [np.empty(self.shapes[d], np.float64) for _ in range(3)]
         _check(lib().ppf_ensemble_download(self._h, int(d), *[x.ctypes.data for x in out]))
         return tuple(out)
+
+    @staticmethod
+    def _ptr_arrays(ptrs):
+        # ptrs: per domain (etaS, etaL, c) addresses -> three C arrays of pointers
+        n = len(ptrs)
+        return [(ctypes.c_void_p * n)(*[int(p[f]) for p in ptrs]) for f in range(3)]
+
+    def upload_from_all(self, ptrs):
+        """Every domain from raw host pointers (e.g. pinned buffers) in one
+        call: ptrs[d] = (etaS, etaL, c) addresses of domain d."""
+        if len(ptrs) != len(self.shapes):
+            raise ValueError("one (etaS, etaL, c) triple per domain")
+        _check(lib().ppf_ensemble_upload_all(self._h, *self._ptr_arrays(ptrs)))
+
+    def download_into_all(self, ptrs):
+        if len(ptrs) != len(self.shapes):
+            raise ValueError("one (etaS, etaL, c) triple per domain")
+        _check(lib().ppf_ensemble_download_all(self._h, *self._ptr_arrays(ptrs)))
+
+    def upload_all(self, states):
+        """Every domain in one call: states[d] = (etaS, etaL, c)."""
+        arrs = [[_c64(x) for x in st] for st in states]
+        for d, a in enumerate(arrs):
+            if any(x.shape != self.shapes[d] for x in a):
+                raise ValueError(f"field shape of domain {d} does not match")
+        self.upload_from_all([[x.ctypes.data for x in a] for a in arrs])
+
+    def download_all(self):
+        out = [tuple(np.empty(s, np.float64) for _ in range(3)) for s in self.shapes]
+        self.download_into_all([[x.ctypes.data for x in o] for o in out])
+        return out
 
     def step(self, n=1):
         _check(lib().ppf_ensemble_step(self._h, int(n)))

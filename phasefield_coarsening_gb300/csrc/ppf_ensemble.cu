@@ -72,6 +72,8 @@ struct ppf_ensemble {
     std::vector<int> order;      // table entry k describes domain order[k]: largest domains first
     DomainDesc *dtable;          // device
     double **ddres;              // device: each domain's dres pointer
+    IoDesc *dio;                 // device: each domain's batched-I/O descriptor (domain order)
+    int64_t max_cells;           // cells of the largest domain
     double *partials;            // 3 doubles per work item
     int partials_cap;
     int items[3];                // work items of the edge-tile [0], whole-tile [1] and every-tile [2] launches
@@ -186,6 +188,7 @@ extern "C" int ppf_ensemble_destroy(ppf_ensemble *e) {
     for (ppf_ctx *c : e->dom) ppf_destroy(c);
     if (e->dtable) cudaFree(e->dtable);
     if (e->ddres) cudaFree(e->ddres);
+    if (e->dio) cudaFree(e->dio);
     if (e->partials) cudaFree(e->partials);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
@@ -229,6 +232,7 @@ extern "C" int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, 
     cudaError_t ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaMalloc(&e->dtable, (size_t)n * sizeof(DomainDesc));
     if (ce == cudaSuccess) ce = cudaMalloc(&e->ddres, (size_t)n * sizeof(double *));
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->dio, (size_t)n * sizeof(IoDesc));
     if (ce != cudaSuccess) {
         ppf_ensemble_destroy(e);
         return err_(PPF_ECUDA, "ensemble setup: %s", cudaGetErrorString(ce));
@@ -245,6 +249,22 @@ extern "C" int ppf_ensemble_create(int n, const int *dims, const ppf_params *p, 
     for (int k = 0; k < n; ++k) h[(size_t)k] = e->dom[(size_t)e->order[(size_t)k]]->dres;
     for (int d = 0; d < n; ++d) e->dom[(size_t)d]->stream = e->stream;   // one stream orders every domain's work
     ce = cudaMemcpy(e->ddres, h.data(), (size_t)n * sizeof(double *), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) {
+        std::vector<IoDesc> io((size_t)n);
+        for (int d = 0; d < n; ++d) {
+            const ppf_ctx *x = e->dom[(size_t)d];
+            IoDesc &t = io[(size_t)d];
+            memset(&t, 0, sizeof t);
+            t.g = x->g;
+            t.staging = x->staging;
+            for (int b = 0; b < 2; ++b)
+                for (int f = 0; f < 3; ++f) t.fld[b][f] = x->fld[b][f];
+            t.dres = x->dres;
+            const int64_t cells = (int64_t)x->nz * x->ny * x->nx;
+            if (cells > e->max_cells) e->max_cells = cells;
+        }
+        ce = cudaMemcpy(e->dio, io.data(), io.size() * sizeof(IoDesc), cudaMemcpyHostToDevice);
+    }
     if (ce != cudaSuccess) {
         ppf_ensemble_destroy(e);
         return err_(PPF_ECUDA, "ensemble setup: %s", cudaGetErrorString(ce));
@@ -290,6 +310,64 @@ extern "C" int ppf_ensemble_download(ppf_ensemble *e, int d, double *etaS, doubl
     int rc = check_domain(e, d);
     if (rc) return rc;
     return ppf_download(e->dom[(size_t)d], etaS, etaL, c);
+}
+
+extern "C" int ppf_ensemble_upload_all(ppf_ensemble *e, const double *const *etaS, const double *const *etaL,
+                                       const double *const *c) {
+    if (!e || !etaS || !etaL || !c) return err_(PPF_EINVAL, "null argument");
+    for (int d = 0; d < e->n; ++d)
+        if (!etaS[d] || !etaL[d] || !c[d]) return err_(PPF_EINVAL, "null array of domain %d", d);
+    // every domain's copies, then one conversion launch for all domains
+    // (which also clears their increment sums), then one synchronisation
+    for (int d = 0; d < e->n; ++d) {
+        ppf_ctx *x = e->dom[(size_t)d];
+        const size_t n = (size_t)x->nz * x->ny * x->nx;
+        ECU(cudaMemcpyAsync(x->staging, etaS[d], n * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        ECU(cudaMemcpyAsync(x->staging + n, etaL[d], n * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        ECU(cudaMemcpyAsync(x->staging + 2 * n, c[d], n * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    }
+    if (e->prec == PPF_F32) ECU(launch_pack_multi<float>(e->dio, e->n, e->max_cells, e->stream));
+    else ECU(launch_pack_multi<double>(e->dio, e->n, e->max_cells, e->stream));
+    for (ppf_ctx *x : e->dom) {
+        x->cur_eta = x->cur_c = 0;
+        x->uploaded = 1;
+        x->steps = 0;
+    }
+    e->parity = 0;
+    ECU(cudaStreamSynchronize(e->stream));
+    return PPF_OK;
+}
+
+extern "C" int ppf_ensemble_download_all(ppf_ensemble *e, double *const *etaS, double *const *etaL,
+                                         double *const *c) {
+    if (!e || !etaS || !etaL || !c) return err_(PPF_EINVAL, "null argument");
+    bool together = true;                      // every domain's state in buffer `parity`
+    for (int d = 0; d < e->n; ++d) {
+        const ppf_ctx *x = e->dom[(size_t)d];
+        if (!etaS[d] || !etaL[d] || !c[d]) return err_(PPF_EINVAL, "null array of domain %d", d);
+        if (!x->uploaded) return err_(PPF_ESTATE, "domain %d has no uploaded state", d);
+        together = together && x->cur_eta == e->parity && x->cur_c == e->parity;
+    }
+    if (!together) {                           // a domain was stepped on its own
+        for (int d = 0; d < e->n; ++d) {
+            const int rc = ppf_download(e->dom[(size_t)d], etaS[d], etaL[d], c[d]);
+            if (rc) return rc;
+        }
+        return PPF_OK;
+    }
+    // one conversion launch for all domains, then every domain's copies, then
+    // one synchronisation
+    if (e->prec == PPF_F32) ECU(launch_unpack_multi<float>(e->dio, e->n, e->max_cells, e->parity, e->stream));
+    else ECU(launch_unpack_multi<double>(e->dio, e->n, e->max_cells, e->parity, e->stream));
+    for (int d = 0; d < e->n; ++d) {
+        ppf_ctx *x = e->dom[(size_t)d];
+        const size_t n = (size_t)x->nz * x->ny * x->nx;
+        ECU(cudaMemcpyAsync(etaS[d], x->staging, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+        ECU(cudaMemcpyAsync(etaL[d], x->staging + n, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+        ECU(cudaMemcpyAsync(c[d], x->staging + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    }
+    ECU(cudaStreamSynchronize(e->stream));
+    return check_device_error(e->dom[0]);
 }
 
 extern "C" int ppf_ensemble_reduce(ppf_ensemble *e, int d, ppf_stats *out) {

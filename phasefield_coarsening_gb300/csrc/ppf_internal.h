@@ -72,6 +72,24 @@ cudaError_t launch_pack(const Geom &g, const double *src3, Fields<T> dst, cudaSt
 template <typename T>
 cudaError_t launch_unpack(const Geom &g, Fields<const T> src, double *dst3, cudaStream_t s);
 
+// One domain of a batched pack / unpack (device table): its geometry, its
+// compact float64 staging array (3 fields), its two state buffers and its
+// device results (the increment sums a fresh upload clears).
+struct IoDesc {
+    Geom g;
+    double *staging;
+    void *fld[2][3];
+    double *dres;
+};
+
+// Pack every domain's staging into its buffer 0 (clearing its increment
+// sums), or unpack every domain's buffer `buf` into its staging: one launch
+// for `n` domains (grid y = domain), the largest holding max_cells cells.
+template <typename T>
+cudaError_t launch_pack_multi(const IoDesc *table, int n, int64_t max_cells, cudaStream_t s);
+template <typename T>
+cudaError_t launch_unpack_multi(const IoDesc *table, int n, int64_t max_cells, int buf, cudaStream_t s);
+
 // Observables of a state: per-CTA partial sums of
 // {mass, solid, solid_cells, free energy, nonfinite} into partials[5*b+i].
 template <typename T>

@@ -108,6 +108,52 @@ static int grid_for(int64_t n, int nt) {
 }
 
 template <typename T>
+__global__ void pack_multi_kernel(const IoDesc *__restrict__ table) {
+    const IoDesc &d = table[blockIdx.y];
+    const Geom g = d.g;
+    const Fields<T> dst = {(T *)d.fld[0][0], (T *)d.fld[0][1], (T *)d.fld[0][2]};
+    const double *src = d.staging;
+    if (blockIdx.x == 0 && threadIdx.x < 3) d.dres[threadIdx.x] = 0.0;
+    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % g.nx);
+        const int y = (int)((i / g.nx) % g.ny);
+        const int z = (int)(i / ((int64_t)g.nx * g.ny));
+        store_with_ghosts(g, dst, x, y, z, (T)src[i], (T)src[n + i], (T)src[2 * n + i], false);
+    }
+}
+
+template <typename T>
+__global__ void unpack_multi_kernel(const IoDesc *__restrict__ table, int buf) {
+    const IoDesc &d = table[blockIdx.y];
+    const Geom g = d.g;
+    const T *sS = (const T *)d.fld[buf][0], *sL = (const T *)d.fld[buf][1], *sC = (const T *)d.fld[buf][2];
+    double *dst = d.staging;
+    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % g.nx);
+        const int y = (int)((i / g.nx) % g.ny);
+        const int z = (int)(i / ((int64_t)g.nx * g.ny));
+        const int64_t j = g.at(x, y, z);
+        dst[i] = (double)sS[j];
+        dst[n + i] = (double)sL[j];
+        dst[2 * n + i] = (double)sC[j];
+    }
+}
+
+template <typename T>
+cudaError_t launch_pack_multi(const IoDesc *table, int n, int64_t max_cells, cudaStream_t s) {
+    pack_multi_kernel<T><<<dim3((unsigned)grid_for(max_cells, 256), (unsigned)n), 256, 0, s>>>(table);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_unpack_multi(const IoDesc *table, int n, int64_t max_cells, int buf, cudaStream_t s) {
+    unpack_multi_kernel<T><<<dim3((unsigned)grid_for(max_cells, 256), (unsigned)n), 256, 0, s>>>(table, buf);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_pack(const Geom &g, const double *src3, Fields<T> dst, cudaStream_t s) {
     pack_kernel<T><<<grid_for((int64_t)g.nx * g.ny * g.nz, 256), 256, 0, s>>>(g, src3, dst);
     return cudaGetLastError();
@@ -203,6 +249,10 @@ template cudaError_t launch_pack<float>(const Geom &, const double *, Fields<flo
 template cudaError_t launch_pack<double>(const Geom &, const double *, Fields<double>, cudaStream_t);
 template cudaError_t launch_unpack<float>(const Geom &, Fields<const float>, double *, cudaStream_t);
 template cudaError_t launch_unpack<double>(const Geom &, Fields<const double>, double *, cudaStream_t);
+template cudaError_t launch_pack_multi<float>(const IoDesc *, int, int64_t, cudaStream_t);
+template cudaError_t launch_pack_multi<double>(const IoDesc *, int, int64_t, cudaStream_t);
+template cudaError_t launch_unpack_multi<float>(const IoDesc *, int, int64_t, int, cudaStream_t);
+template cudaError_t launch_unpack_multi<double>(const IoDesc *, int, int64_t, int, cudaStream_t);
 template cudaError_t launch_observe<float>(const Geom &, const CoefD &, Fields<const float>, double *, int,
                                            cudaStream_t);
 template cudaError_t launch_observe<double>(const Geom &, const CoefD &, Fields<const double>, double *, int,

@@ -71,3 +71,30 @@ def test_ensemble_autotune_keeps_state_and_reupload():
         ref, _ = _single(SHAPES[2], states[2], 2, "periodic", "f32", pieces=(2,))
         for a, b in zip(e.download(2), ref):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_ensemble_batched_io_equals_per_domain_io(precision):
+    """ppf_ensemble_upload_all / download_all (one conversion launch for all
+    domains) give the per-domain calls' bits, before and after steps, and
+    after an odd number of steps (state in the second buffer)."""
+    states = [smooth_state(sh, seed=70 + i) for i, sh in enumerate(SHAPES)]
+    with ppf.Ensemble(SHAPES, precision=precision) as a, ppf.Ensemble(SHAPES, precision=precision) as b:
+        a.upload_all(states)
+        for d, st in enumerate(states):
+            b.upload(d, *st)
+        for x, y in zip(a.download_all(), [b.download(d) for d in range(len(SHAPES))]):
+            for p, q in zip(x, y):
+                assert np.array_equal(p, q)
+        for n in (5, 16):
+            a.step(n)
+            b.step(n)
+            got = a.download_all()
+            for d in range(len(SHAPES)):
+                for p, q in zip(got[d], b.download(d)):
+                    assert np.array_equal(p, q), (n, d)
+            ra, rb = a.reduce(2), b.reduce(2)
+            assert ra["sum_dc2"] == rb["sum_dc2"] and ra["steps"] == rb["steps"]
+        # a fresh batched upload restarts every domain (increment sums cleared)
+        a.upload_all(states)
+        assert a.reduce(0)["sum_dc2"] == 0.0 and a.reduce(0)["steps"] == 0

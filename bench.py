@@ -513,10 +513,14 @@ def run_ensemble(args):
     # one host thread each, take turns at the bench steps so that the
     # host-link copies of some overlap the others' stepping (as in the
     # single-domain line).
+    # (plain launches: with programmatic dependent launch, an ensemble's next
+    # step grid holds SM slots while it waits, which the other ensemble's
+    # kernels then wait for)
     extra = []
+    ens.set_tune(tune["zc"], tune["roll"], tune["sched"], 0, tune["split"], tune["tile"])
     for _ in range(ENS_E2E_ENSEMBLES - 1):
         ex = ppf.Ensemble(shapes, prm, bc="periodic", precision="f32")
-        ex.set_tune(tune["zc"], tune["roll"], tune["sched"], tune["pdl"], tune["split"], tune["tile"])
+        ex.set_tune(tune["zc"], tune["roll"], tune["sched"], 0, tune["split"], tune["tile"])
         extra.append(ex)
     pin_in = [[torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in d[:3]] for d in doms]
     pin_out = [[[torch.empty(s, dtype=torch.float64).pin_memory() for _ in range(3)] for s in shapes]

@@ -405,12 +405,15 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def ensemble_measure(doms, steps, warmup, world=1):
+def ensemble_measure(doms, steps, warmup, world=1, launch=None):
     """The ensemble of domains `doms` advanced by one persistent launch per
     time step under CUDA-graph replay, against the same domains stepped one
     context at a time (64 launches per time step).  Host wall-clock around
-    step(n) + sync, so launch overheads count.  Returns (ensemble, section
-    dict, tune); the caller closes the ensemble."""
+    step(n) + sync, so launch overheads count.  `launch` = (z chunk, unroll)
+    fixes the launch choice (work items from the counter, programmatic
+    dependent launch, one launch over every tile, 64 x 16 tiles) instead of
+    the autotuner's.  Returns (ensemble, section dict, tune); the caller
+    closes the ensemble."""
     import numpy as np
 
     import phasefield_coarsening_gb300 as ppf
@@ -421,7 +424,11 @@ def ensemble_measure(doms, steps, warmup, world=1):
     ens = ppf.Ensemble(shapes, prm, bc="periodic", precision="f32")
     for i, (eS, eL, c, _) in enumerate(doms):
         ens.upload(i, eS, eL, c)
-    tune = ens.autotune(trial_steps=5)
+    if launch:
+        ens.set_tune(launch[0], launch[1], 1, 1, 0, 0)
+        tune = ens.get_tune()
+    else:
+        tune = ens.autotune(trial_steps=5)
 
     def timed(step_fn, sync_fn):
         for _ in range(warmup):
@@ -505,7 +512,8 @@ def run_ensemble(args):
     prm = ppf.params_default(dt=DT)
     clocks = ClockSampler(local)
     clocks.start()
-    ens, sec, tune = ensemble_measure(doms, args.steps, args.warmup, world)
+    ens, sec, tune = ensemble_measure(doms, args.steps, args.warmup, world,
+                                      launch=args.launch[:2] if args.launch else None)
     clk = clocks.stop()
 
     # e2e through the C-ABI: every bench step uploads all domains from pinned

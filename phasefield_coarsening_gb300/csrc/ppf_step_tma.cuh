@@ -502,9 +502,10 @@ __global__ void __launch_bounds__(TmaGeo<T, TILE>::NT, 2)
 
         // producer (thread 0): takes the CTA's items and walks their planes,
         // S-2 loads ahead of the consumers.  Items come round-robin
-        // (blockIdx.x, + gridDim.x, ...) or, with a scheduler word pair, from
-        // a global counter in the same chunk-major order, so that a CTA that
-        // runs faster takes more items.  Each item id is published in s_next
+        // (blockIdx.x, + gridDim.x, ...) or, with a scheduler word pair,
+        // blockIdx.x first and then gridDim.x + a global counter, in the same
+        // chunk-major order, so that a CTA that runs faster takes more items
+        // (the grid never exceeds the item count).  Each item id is published in s_next
         // (two slots: an item spans at least three planes, so the producer is
         // never more than one item ahead), written at least two plane
         // barriers before the consumers read it.
@@ -513,7 +514,9 @@ __global__ void __launch_bounds__(TmaGeo<T, TILE>::NT, 2)
         auto take = [&]() {
             int v;
             if (sched) {
-                v = atomicAdd(&sched[0], 1);
+                // a CTA's first item is its own index (no counter round trip before
+                // the first load); later ones come from the counter
+                v = p_seq == 0 ? (int)blockIdx.x : (int)gridDim.x + atomicAdd(&sched[0], 1);
                 if (v >= nitems) {
                     v = nitems;
                     // the last CTA to stop taking items resets the pair for the next launch

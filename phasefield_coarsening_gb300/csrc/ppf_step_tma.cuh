@@ -1,14 +1,16 @@
 // ppf_step_tma.cuh -- the fused explicit step as a TMA-fed, z-marching,
 // persistent sm_103a kernel (instantiated per precision by ppf_step_f32.cu
-// and ppf_step_f64.cu, which compile in parallel).
+// and ppf_step_f64.cu for single domains and by ppf_step_f32_ens.cu and
+// ppf_step_f64_ens.cu for ensembles, which compile in parallel).
 //
 // Replaces, per time step, the reference's BC fill (phasefield.c:1112-1189)
 // and the three passes of sweep_fields (:325-335 pass A, :347-391 pass B,
 // :393-401 pass C) -- or of sweep_fields_c (:406-476) in c-only mode.
 //
 // Data flow of one CTA:
-//   * (z chunk, x-y tile) work items in chunk-major order, dealt round-robin
-//     to a persistent grid; each item is a tile column segment marched up z;
+//   * (z chunk, x-y tile) work items in chunk-major order, taken by the CTAs
+//     of a persistent grid from a global counter (or dealt round-robin);
+//     each item is a tile column segment marched up z;
 //   * thread 0 streams every plane's etaS/etaL/c tile plus a one-cell ring
 //     (a TX+2*XH by TY+2 box per field) from HBM into a S-stage shared ring
 //     with cp.async.bulk.tensor.3d, completion signalled on an mbarrier per
@@ -315,10 +317,10 @@ __device__ __forceinline__ void put_ghost(const Fields<T> &o, I a, T s, T l, T c
     o.c[a] = c;
 }
 
-// Work items are (z chunk, x-y tile) pairs in chunk-major order, dealt
-// round-robin to the persistent CTAs: CTAs resident at the same time march
+// Work items are (z chunk, x-y tile) pairs in chunk-major order, taken in
+// that order by the persistent CTAs: CTAs resident at the same time march
 // the same z window of neighbouring tiles, so the halo rows one tile reads
-// from its neighbours' data are still in L2.
+// from its neighbours' data are mostly still in L2.
 
 // Registers of the own cells of one plane, as pairs (cell i, cell i+H) of
 // the thread's column of CY = 2H cells: with that pairing the y neighbours
@@ -950,8 +952,9 @@ void step_tile(int *tx, int *ty, int tile) {
 template <typename T>
 int step_tile_shapes() { return kTileShapes<T>; }
 
-// Launch shape.  Work items are (z chunk, tile) pairs dealt round-robin to
-// a persistent grid of `slots` CTAs (occupancy x SMs).  The chunk length
+// Launch shape (the model behind the default z chunk).  Work items are
+// (z chunk, tile) pairs dealt round-robin to a persistent grid of `slots`
+// CTAs (occupancy x SMs).  The chunk length
 // zc is chosen to minimise the busiest CTA's load count -- its planes plus
 // two halo planes per item -- so that the resident CTAs end together;
 // *zc_out receives it (for the first tile shape).

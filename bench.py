@@ -136,6 +136,29 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def host_link_gbs(pinned_src, pinned_dst):
+    """Pinned host <-> device copy rates of this host (GB/s, best of 3 copies
+    of one field array each way), which bound the end-to-end line."""
+    import torch
+
+    dev = torch.empty(pinned_src.numel(), dtype=pinned_src.dtype, device="cuda")
+    out = {}
+    for name, fn in (("h2d", lambda: dev.copy_(pinned_src.view(-1), non_blocking=True)),
+                     ("d2h", lambda: pinned_dst.view(-1).copy_(dev, non_blocking=True))):
+        best = None
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        out[name] = round(dev.numel() * dev.element_size() / (best * 1e-3) / 1e9, 1)
+    del dev
+    return out
+
+
 def read_profile_traffic():
     """dram bytes per launch of the f32 step from the committed ncu summary."""
     p = os.path.join(REPO, "profiles", "step_f32_spheres256.md")
@@ -361,6 +384,7 @@ def run_ours(args):
         sx.close()
     e2e_s = max_over_ranks(e2e_s)
     e2e_value = job_glups(world, cells, INNER * args.steps, e2e_s)
+    link = host_link_gbs(host[0], outh[0][0])
 
     if rank == 0:
         hbm, src = peaks()
@@ -382,7 +406,7 @@ def run_ours(args):
                          "kernel": "step_tma_kernel<float> (fused step, TMA-fed)", "algorithmic_bytes_per_launch": ALG_BYTES_F32 * cells,
                          "avg_launch_us": round(step_ms * 1e3, 2), "peak_source": src},
             "e2e": {"value": round(e2e_value, 3), "unit": "GLUPS", "h2d_bytes_per_step": 3 * cells * 8,
-                    "d2h_bytes_per_step": 3 * cells * 8 + 8 * 8,
+                    "d2h_bytes_per_step": 3 * cells * 8 + 8 * 8, "host_link_gbs": link,
                     "how": "ppf_upload (pinned float64 host arrays) + 100 ppf_step + ppf_reduce + ppf_download "
                            f"per bench step; {E2E_CONTEXTS} contexts on their own streams, one host thread each, take "
                            "turns at the bench steps so that copies overlap stepping; wall clock over all steps"},

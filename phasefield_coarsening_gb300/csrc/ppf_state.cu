@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "ppf_internal.h"
 
@@ -171,12 +172,32 @@ cudaError_t launch_unpack(const Geom &g, Fields<const T> src, double *dst3, cuda
 // derivative is the bracket of phasefield.c:360-373):
 //   m f0(etaS, etaL) + kappa/2 |grad eta|^2 (forward differences) + hS fS + (1-hS) fL
 
+// A float sum carried with its rounding error (Knuth's TwoSum): about 48
+// bits, enough for per-thread partial sums of FP32 cell terms; FP32 adds are
+// far cheaper than FP64 ones on this GPU.
+struct FSum {
+    float hi, lo;
+};
+__device__ __forceinline__ void fsum_add(FSum &a, float x) {
+    const float s = a.hi + x;
+    const float bp = s - a.hi;
+    const float err = (a.hi - (s - bp)) + (x - bp);
+    a.hi = s;
+    a.lo += err;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) observe_kernel(Geom g, CoefD kd, Fields<const T> f, double *partials) {
     const T AS = (T)kd.AS, AL = (T)kd.AL, dA = (T)kd.dA, cS0 = (T)kd.cS0, cL0 = (T)kd.cL0;
     const T CS = (T)kd.CS, CL = (T)kd.CL, tmp2 = (T)kd.tmp2, m = (T)kd.m, gam = (T)kd.gamma;
     const T kg = (T)kd.kappa_h2_half;
+    constexpr bool F32 = std::is_same<T, float>::value;
     double acc[5] = {0, 0, 0, 0, 0};
+    // FP32 state: the solid fraction and the free energy are summed per
+    // thread as compensated float sums (the solute mass stays an FP64 sum of
+    // the stored values, exact to rounding); FP64 state: FP64 throughout
+    FSum hsum = {0.f, 0.f}, fsum = {0.f, 0.f};
+    int nsolid = 0, nbad = 0;
     // one block per x row (grid-stride over rows): no per-cell index division
     const int nrows = g.ny * g.nz;
     for (int rr = blockIdx.x; rr < nrows; rr += gridDim.x) {
@@ -185,7 +206,7 @@ __global__ void __launch_bounds__(256) observe_kernel(Geom g, CoefD kd, Fields<c
             const int64_t j = j0 + x;
             const T eS = f.eS[j], eL = f.eL[j], c = f.c[j];
             if (!isfinite(eS) || !isfinite(eL) || !isfinite(c)) {
-                acc[4] += 1.0;
+                ++nbad;
                 continue;
             }
             // +x/+y/+z neighbours read through the ghost layer (periodic wrap or no-flux copy)
@@ -203,13 +224,27 @@ __global__ void __launch_bounds__(256) observe_kernel(Geom g, CoefD kd, Fields<c
             const T fS = T(0.5) * AS * (cSp - cS0) * (cSp - cS0) + CS;
             const T fL = T(0.5) * AL * (cLp - cL0) * (cLp - cL0) + CL;
             acc[0] += (double)c;
-            acc[1] += (double)h;
-            acc[2] += eS > T(0.5) ? 1.0 : 0.0;
-            // the terms differ by orders of magnitude (the parabola offsets CS, CL
-            // against gradient and well terms): summed in double
-            acc[3] += ((double)(m * f0) + (double)(kg * gr)) + ((double)(h * fS) + (double)((T(1) - h) * fL));
+            nsolid += eS > T(0.5) ? 1 : 0;
+            if constexpr (F32) {
+                fsum_add(hsum, h);
+                // the terms differ by orders of magnitude (the parabola offsets
+                // CS, CL against gradient and well terms): each added on its own
+                fsum_add(fsum, m * f0);
+                fsum_add(fsum, kg * gr);
+                fsum_add(fsum, h * fS);
+                fsum_add(fsum, (T(1) - h) * fL);
+            } else {
+                acc[1] += (double)h;
+                acc[3] += ((double)(m * f0) + (double)(kg * gr)) + ((double)(h * fS) + (double)((T(1) - h) * fL));
+            }
         }
     }
+    if constexpr (F32) {
+        acc[1] = (double)hsum.hi + (double)hsum.lo;
+        acc[3] = (double)fsum.hi + (double)fsum.lo;
+    }
+    acc[2] = (double)nsolid;
+    acc[4] = (double)nbad;
     acc[3] *= kd.vol;
     block_sum_store<256, 5>(acc, partials, blockIdx.x);
 }
